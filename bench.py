@@ -1,0 +1,450 @@
+"""Benchmark of the GB300 Lloyd k-means engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--form auto|plain|mixed-bf16|mixed-fp16] [--workload c3|c2|c1]
+
+A step is one Lloyd iteration (fused assignment + accumulation, reduction,
+relocation gate, division, shift test) over the whole synthetic data set.
+Default workload (c3): n = 10,000,000 samples x d = 64 float32 features,
+k = 1024 clusters, Gaussian blobs (1024 centres uniform in [-5, 5]^64,
+per-blob sigma uniform in [0.5, 2.0], seed 2), seeded random-row init.
+
+value    iterations/s with X already resident in HBM, timed with CUDA events
+         on the fit's stream over exactly K steps (max over ranks).
+e2e      the same metric through the drop-in Python surface
+         (kmeans_lloyd_driver) with host buffers: pinned host -> device copies
+         of X, weights and initial centroids, K iterations, and the device ->
+         host read of labels, centroids and inertia, all inside the timed region.
+roofline for the dominant kernel (assignment + accumulation), from its CUDA
+         event times inside the timed region.
+cpu_baseline  the CPU oracle (C++/OpenMP restatement of the reference path) on
+         a bounded sample of the same workload, scaled to iterations/s.
+
+--impl reference times the reference's algorithm on the host cores.  The
+reference itself (SYCL/DPC++ + dpctl) cannot be built here, so its CPU
+restatement (oracle/kmref.cpp) stands in for it.
+
+Multi-GPU (torchrun): the Lloyd loop is not sharded in this build; each rank
+runs an independent replica and value counts the iterations of all replicas
+("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+METRIC = "Lloyd iter/s + %roofline (10M×64, k=1024), mixed vs FP32; serve p50/p99"
+
+WORKLOADS = {
+    # name: n, d, n_centers, k, box, std (scalar or (lo, hi) per blob), seed, far_first
+    "c3": dict(n=10_000_000, d=64, centers=1024, k=1024, box=(-5.0, 5.0), std=(0.5, 2.0), seed=2,
+               far_first=False, desc="10M x 64 float32 Gaussian blobs, k=1024, random-row init"),
+    "c2": dict(n=5_000_000, d=14, centers=127, k=127, box=(-10.0, 10.0), std=1.5, seed=1,
+               far_first=True, desc="5M x 14 float32 Gaussian blobs, k=127, centroid 0 = 1e3*ones"),
+    "c1": dict(n=50_000, d=14, centers=16, k=16, box=(-10.0, 10.0), std=1.0, seed=0,
+               far_first=False, desc="50k x 14 float32 Gaussian blobs, k=16"),
+}
+
+FORMS = {"plain": 0, "mixed-bf16": 1, "mixed-fp16": 2}
+
+
+# ---------------------------------------------------------------------------
+# synthetic data (shared with the tests)
+# ---------------------------------------------------------------------------
+def make_blobs(n, d, n_centers, center_box, std, seed, dtype=np.float32):
+    """Isotropic Gaussian blobs with equal blob sizes, rows shuffled.
+
+    Returns (X_t (d, n) C-contiguous, centers (n_centers, d), blob_of_row (n,)).
+    `std` is a scalar, a (lo, hi) tuple (per-blob sigma uniform in [lo, hi]) or
+    an array of per-blob standard deviations.
+    """
+    rng = np.random.default_rng(seed)
+    centers = rng.uniform(center_box[0], center_box[1], size=(n_centers, d))
+    if isinstance(std, tuple):
+        stds = rng.uniform(std[0], std[1], size=n_centers)
+    else:
+        stds = np.broadcast_to(np.asarray(std, dtype=np.float64), (n_centers,))
+    blob = rng.permutation(n) % n_centers
+    X_t = np.empty((d, n), dtype=dtype)
+    chunk = 1 << 20
+    for i0 in range(0, n, chunk):
+        b = blob[i0:i0 + chunk]
+        noise = rng.standard_normal((b.size, d), dtype=np.float32)
+        X_t[:, i0:i0 + chunk] = (centers[b] + noise * stds[b, None]).T.astype(dtype)
+    return X_t, centers, blob
+
+
+def random_row_init(X_t, k, seed, far_first=False):
+    """Initial centroids (d, k): X rows at seeded indices without replacement.
+
+    far_first replaces centroid 0 by 1e3 * ones (forces an empty cluster)."""
+    rng = np.random.default_rng(seed + 7919)
+    idx = rng.choice(X_t.shape[1], size=k, replace=False)
+    C = np.ascontiguousarray(X_t[:, idx])
+    if far_first:
+        C[:, 0] = 1e3
+    return C
+
+
+def workload_data(name):
+    w = WORKLOADS[name]
+    X_t, _, _ = make_blobs(w["n"], w["d"], w["centers"], w["box"], w["std"], w["seed"])
+    C0 = random_row_init(X_t, w["k"], w["seed"], far_first=w["far_first"])
+    return X_t, C0
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+    def __init__(self, gpu_id=None, interval_ms=50):
+        self.cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                    f"-lms={interval_ms}"]
+        if gpu_id:
+            self.cmd.append(f"--id={gpu_id}")
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(self.cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(self.NAMES, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle timing (cpu_baseline and the reference arm)
+# ---------------------------------------------------------------------------
+def cpu_step_time(X_t, C0, n_s):
+    from oracle import kmref
+
+    Xs = np.ascontiguousarray(X_t[:, :n_s])
+    w = np.ones(n_s, X_t.dtype)
+    t0 = time.perf_counter()
+    kmref.fused_lloyd_single_step(Xs, w, C0)
+    return time.perf_counter() - t0
+
+
+def calibrate_cpu_sample(X_t, C0, target_s):
+    n = X_t.shape[1]
+    n_s = min(n, 20_000)
+    t = cpu_step_time(X_t, C0, n_s)
+    n_s = int(min(n, max(1000, n_s * target_s / max(t, 1e-6))))
+    return n_s
+
+
+def cpu_baseline(X_t, C0, target_s=10.0):
+    from oracle import kmref
+
+    n = X_t.shape[1]
+    n_s = calibrate_cpu_sample(X_t, C0, target_s)
+    t = cpu_step_time(X_t, C0, n_s)
+    return {"value": (n_s / n) / t, "unit": "iter/s", "cores": kmref.num_threads(), "kind": "port",
+            "sample": f"one Lloyd step (assignment + accumulation) over the first {n_s} of {n} "
+                      f"samples, scaled by n/{n_s}; oracle/kmref.cpp, OpenMP"}
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (replicas)
+# ---------------------------------------------------------------------------
+def dist_setup(n_gpus):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def all_max(world, v):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, world, rank):
+    """CPU reference arm: the reference algorithm on the host cores."""
+    from oracle import kmref
+
+    if rank != 0:
+        return
+    w = WORKLOADS[args.workload]
+    X_t, C0 = workload_data(args.workload)
+    n = X_t.shape[1]
+    n_s = calibrate_cpu_sample(X_t, C0, target_s=1.5)
+    for _ in range(args.warmup):
+        cpu_step_time(X_t, C0, n_s)
+    times = [cpu_step_time(X_t, C0, n_s) for _ in range(args.steps)]
+    t_step = sum(times) / len(times)
+    value = (n_s / n) / t_step
+    sample = (f"each step: one Lloyd step (assignment + accumulation) over the first {n_s} of {n} "
+              f"samples, scaled by n/{n_s}; the reference (SYCL/DPC++) cannot be built here, so its "
+              f"C++ restatement oracle/kmref.cpp runs with OpenMP on all host threads")
+    line = {
+        "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": args.workload, "desc": w["desc"], "n": w["n"], "d": w["d"], "k": w["k"]},
+        "cpu_baseline": {"value": value, "unit": "iter/s", "cores": kmref.num_threads(),
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, world, rank, local):
+    import torch
+
+    import kmeans_dpcpp_gb300 as kdp
+    from kmeans_dpcpp_gb300 import capi
+
+    torch.cuda.set_device(local)
+    L = capi.lib()
+    w = WORKLOADS[args.workload]
+    n, d, k = w["n"], w["d"], w["k"]
+    X_t, C0 = workload_data(args.workload)
+    form_name = "plain" if args.form == "auto" else args.form
+    form = FORMS[form_name]
+
+    # ---- device-resident timing through a fit session ----
+    stream = torch.cuda.Stream()
+    Xg = torch.from_numpy(X_t).cuda()
+    wg = torch.ones(n, dtype=torch.float32, device="cuda")
+    cur = torch.from_numpy(C0.copy()).cuda()
+    res_c = torch.empty_like(cur)
+    lab = torch.empty(n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    fit = ctypes.c_void_p()
+    max_iter = args.warmup + args.steps + 1
+    capi.check(L.kmc_fit_create_f32_i32(Xg.data_ptr(), wg.data_ptr(), cur.data_ptr(), lab.data_ptr(),
+                                        res_c.data_ptr(), n, d, k, 0.0, max_iter, form,
+                                        stream.cuda_stream, ctypes.byref(fit)))
+    capi.check(L.kmc_fit_set_profiling(fit, 1))
+    capi.check(L.kmc_fit_step(fit, args.warmup))
+    stream.synchronize()
+    ms0, c0 = ctypes.c_double(), ctypes.c_int64()
+    capi.check(L.kmc_fit_phase_time(fit, 0, ctypes.byref(ms0), ctypes.byref(c0)))
+    l0 = ctypes.c_int64()
+    capi.check(L.kmc_fit_launch_count(fit, ctypes.byref(l0)))
+
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        pass
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(uuid) as clk:
+        time.sleep(0.15)
+        ev0.record(stream)
+        capi.check(L.kmc_fit_step(fit, args.steps))
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+        barrier(world)
+        time.sleep(0.05)
+    elapsed_ms = ev0.elapsed_time(ev1)
+    elapsed_ms = all_max(world, elapsed_ms)
+    ms1, c1 = ctypes.c_double(), ctypes.c_int64()
+    capi.check(L.kmc_fit_phase_time(fit, 0, ctypes.byref(ms1), ctypes.byref(c1)))
+    l1 = ctypes.c_int64()
+    capi.check(L.kmc_fit_launch_count(fit, ctypes.byref(l1)))
+    it, done, shift = ctypes.c_int64(), ctypes.c_int(), ctypes.c_double()
+    capi.check(L.kmc_fit_status(fit, ctypes.byref(it), ctypes.byref(done), ctypes.byref(shift)))
+    capi.check(L.kmc_fit_destroy(fit))
+    assert it.value == args.warmup + args.steps, (it.value, "the loop stopped early")
+
+    ms_per_step = elapsed_ms / args.steps
+    value = world * args.steps / (elapsed_ms / 1000.0)
+
+    # ---- roofline of the dominant kernel ----
+    peaks, peak_src = measured_peaks()
+    kern_ms = (ms1.value - ms0.value) / max(1, c1.value - c0.value)
+    flops = 2.0 * n * k * d
+    if form_name == "plain":
+        sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+        clk_mhz = clk.summary()["sm_max_mhz"] or 2070.0
+        peak_tf = sm_count * 128 * 2 * clk_mhz * 1e6 / 1e12
+        roofline = {"bound": "fp32", "achieved": flops / (kern_ms * 1e-3) / 1e12, "peak": peak_tf,
+                    "unit": "TFLOP/s", "traffic": None,
+                    "peak_source": f"nominal FP32 FFMA rate ({sm_count} SMs x 128 lanes x 2 flop "
+                                   f"x {clk_mhz:.0f} MHz); the plain form runs on the FP32 pipe",
+                    "kernel": "tile_kernel (fused assignment + accumulation)",
+                    "kernel_ms": kern_ms, "flops_per_launch": flops}
+    else:
+        peak_tf = peaks.get("bf16_tflops_sustained", 1700.0)
+        roofline = {"bound": "tensor", "achieved": flops / (kern_ms * 1e-3) / 1e12, "peak": peak_tf,
+                    "unit": "TFLOP/s", "traffic": None,
+                    "peak_source": f"bf16_tflops_sustained of {peak_src} MEASURED_PEAKS.json",
+                    "kernel": "mixed assignment + accumulation", "kernel_ms": kern_ms,
+                    "flops_per_launch": flops}
+    roofline["frac"] = roofline["achieved"] / roofline["peak"]
+
+    # ---- end to end through the drop-in surface, host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        X_h = torch.from_numpy(X_t).pin_memory()
+        w_h = torch.ones(n, dtype=torch.float32).pin_memory()
+        C_h = torch.from_numpy(C0.copy()).pin_memory()
+        lab_h = torch.empty(n, dtype=torch.int32).pin_memory()
+        Cres_h = torch.empty_like(C_h).pin_memory()
+        Xd = torch.empty_like(Xg)
+        wd = torch.empty_like(wg)
+        Cd = torch.empty_like(cur)
+        Crd = torch.empty_like(cur)
+        labd = torch.empty_like(lab)
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Xd.copy_(X_h, non_blocking=True)
+        wd.copy_(w_h, non_blocking=True)
+        Cd.copy_(C_h, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        n_iter, inertia = kdp.kmeans_lloyd_driver(Xd, wd, Cd, labd, Crd, 0.0, False, args.steps, 8, 128,
+                                                  0.7, None)
+        lab_h.copy_(labd)
+        Cres_h.copy_(Crd)
+        torch.cuda.synchronize()
+        t_e2e = time.perf_counter() - t0
+        t_e2e = all_max(world, t_e2e)
+        assert n_iter == args.steps
+        h2d = X_t.nbytes + 4 * n + C0.nbytes
+        d2h = 4 * n + C0.nbytes + 4
+        e2e = {"value": world * n_iter / t_e2e, "unit": "iter/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h,
+               "note": "one kmeans_lloyd_driver call of K iterations (tol=0) with pinned-host "
+                       "copies of X, weights, init centroids in and labels, centroids, inertia "
+                       "out; bytes are per call"}
+        del Xd, X_h
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if form_name == "plain" else form_name.split("-")[1],
+        "data": "synthetic",
+        "config": {"workload": args.workload, "desc": w["desc"], "n": n, "d": d, "k": k,
+                   "form": form_name, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (X is %.2f GB)" % (X_t.nbytes / 1e9)},
+        "roofline": roofline,
+        "clocks": clk.summary(),
+        "gpu_launches": int(l1.value - l0.value),
+        "e2e": e2e,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(X_t, C0, target_s=args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--form", choices=["auto"] + sorted(FORMS), default="auto")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c3")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        rank = int(os.environ.get("RANK", "0"))
+        run_reference(args, world, rank)
+        return
+    world, rank, local = dist_setup(args.gpus)
+    run_gb300(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,440 @@
+/*
+ * kmeans_gb300.h -- C ABI of the GB300 (sm_103a) Lloyd k-means engine.
+ *
+ * This is the drop-in boundary for the pybind11 surface of kmeans_dpcpp
+ * (python_api/_kmeans_lloyd.cpp).  Each entry point replaces one templated
+ * SYCL host function that the reference's pybind11 wrappers dispatch to; the
+ * comment above each group cites the wrapper (python_api/_kmeans_lloyd.cpp)
+ * and the kernel header (src/*.hpp) it replaces.
+ *
+ * Conventions
+ *  - All array arguments are device pointers to C-contiguous arrays, in the
+ *    layouts of the reference: X_t is (n_features, n_samples), centroid
+ *    matrices are (n_features, n_clusters), private copies are
+ *    (n_copies, n_features, n_clusters) and (n_copies, n_clusters).
+ *  - Suffix _f32/_f64 selects dataT (float/double), _i32/_i64 selects indT.
+ *  - `stream` is a cudaStream_t (0 = legacy default stream).  Every call is
+ *    asynchronous on that stream unless documented as blocking, exactly like
+ *    the reference's submit-and-return-event pattern.
+ *  - work_group_size and centroids_window_height are accepted for API
+ *    compatibility; the engine picks its own tile shapes.
+ *  - Every function returns KMC_OK (0) or a KMC_ERR_* code and never throws;
+ *    kmc_last_error() returns a message for the calling thread.
+ */
+#ifndef KMEANS_GB300_H
+#define KMEANS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *kmc_stream_t; /* ABI-identical to cudaStream_t */
+typedef struct CUevent_st *kmc_event_t;   /* ABI-identical to cudaEvent_t  */
+
+#define KMC_OK 0
+#define KMC_ERR_INVALID_ARGUMENT 1
+#define KMC_ERR_CUDA 2
+#define KMC_ERR_OUT_OF_MEMORY 3
+#define KMC_ERR_UNSUPPORTED 4
+#define KMC_ERR_DEVICE_TIMEOUT 5
+
+/* Message describing the last failure on the calling thread. */
+const char *kmc_last_error(void);
+/* ABI version of this library. */
+int kmc_abi_version(void);
+
+/* ---- broadcast_divide: X /= y column-wise --------------------------------
+ * replaces py_broadcast_divide (_kmeans_lloyd.cpp:60-105) ->
+ * broadcast_division_kernel (src/util_kernels.hpp:9-41).
+ * divident is (n_rows, n_cols), divisor is (n_cols,). */
+int kmc_broadcast_divide_f32(float *divident, const float *divisor, int64_t n_rows,
+                             int64_t n_cols, int64_t work_group_size, kmc_stream_t stream);
+int kmc_broadcast_divide_f64(double *divident, const double *divisor, int64_t n_rows,
+                             int64_t n_cols, int64_t work_group_size, kmc_stream_t stream);
+
+/* ---- half_l2_norm_squared: y[j] = sum_f X[f,j]^2 / 2 -----------------------
+ * replaces py_half_l2_norm_squared (_kmeans_lloyd.cpp:108-152) ->
+ * half_l2_norm_kernel (src/util_kernels.hpp:47-82). */
+int kmc_half_l2_norm_squared_f32(const float *centroids, float *out, int64_t n_features,
+                                 int64_t n_clusters, int64_t work_group_size,
+                                 kmc_stream_t stream);
+int kmc_half_l2_norm_squared_f64(const double *centroids, double *out, int64_t n_features,
+                                 int64_t n_clusters, int64_t work_group_size,
+                                 kmc_stream_t stream);
+
+/* ---- reduce_centroids_data -------------------------------------------------
+ * replaces py_reduce_centroids_data (_kmeans_lloyd.cpp:155-282) ->
+ * reduce_centroid_data_kernel (src/util_kernels.hpp:87-161).
+ * Empty clusters are appended to out_empty_clusters_list starting at the
+ * current value of *out_n_empty_clusters, in ascending cluster order. */
+int kmc_reduce_centroids_data_f32_i32(const float *cluster_sizes_private_copies,
+                                      const float *centroids_t_private_copies,
+                                      float *out_cluster_sizes, float *out_centroids_t,
+                                      int32_t *out_empty_clusters_list,
+                                      int32_t *out_n_empty_clusters, int64_t n_copies,
+                                      int64_t n_features, int64_t n_clusters,
+                                      int64_t work_group_size, kmc_stream_t stream);
+int kmc_reduce_centroids_data_f32_i64(const float *cluster_sizes_private_copies,
+                                      const float *centroids_t_private_copies,
+                                      float *out_cluster_sizes, float *out_centroids_t,
+                                      int64_t *out_empty_clusters_list,
+                                      int64_t *out_n_empty_clusters, int64_t n_copies,
+                                      int64_t n_features, int64_t n_clusters,
+                                      int64_t work_group_size, kmc_stream_t stream);
+int kmc_reduce_centroids_data_f64_i32(const double *cluster_sizes_private_copies,
+                                      const double *centroids_t_private_copies,
+                                      double *out_cluster_sizes, double *out_centroids_t,
+                                      int32_t *out_empty_clusters_list,
+                                      int32_t *out_n_empty_clusters, int64_t n_copies,
+                                      int64_t n_features, int64_t n_clusters,
+                                      int64_t work_group_size, kmc_stream_t stream);
+int kmc_reduce_centroids_data_f64_i64(const double *cluster_sizes_private_copies,
+                                      const double *centroids_t_private_copies,
+                                      double *out_cluster_sizes, double *out_centroids_t,
+                                      int64_t *out_empty_clusters_list,
+                                      int64_t *out_n_empty_clusters, int64_t n_copies,
+                                      int64_t n_features, int64_t n_clusters,
+                                      int64_t work_group_size, kmc_stream_t stream);
+
+/* ---- compute_threshold: topk-th largest element of data ---------------------
+ * replaces py_compute_threshold (_kmeans_lloyd.cpp:284-337) ->
+ * compute_threshold_kernel (src/util_kernels.hpp:163-206) and the
+ * iterative_merge_sort it calls (src/iterative_merge_sort.hpp:204-368),
+ * by a radix select.  topk == 0 is a no-op, as in the reference. */
+int kmc_compute_threshold_f32(const float *data, int64_t n_samples, int64_t topk,
+                              float *threshold, kmc_stream_t stream);
+int kmc_compute_threshold_f64(const double *data, int64_t n_samples, int64_t topk,
+                              double *threshold, kmc_stream_t stream);
+
+/* ---- select_samples_far_from_centroid ---------------------------------------
+ * replaces py_select_samples_far_from_centroid (_kmeans_lloyd.cpp:339-441) ->
+ * select_samples_far_from_centroid_kernel (src/util_kernels.hpp:211-297).
+ * Indices with distance > threshold go to the front (ordered so that
+ * selected[n_gt-1-r] is the r-th farthest, ties by lowest index), indices with
+ * distance == threshold go to the back (selected[n-1], selected[n-2], ... in
+ * ascending index order).  The counters are incremented from their current
+ * values, as in the reference. */
+int kmc_select_samples_far_from_centroid_f32_i32(int64_t n_selected,
+                                                 const float *distance_to_centroid,
+                                                 const float *threshold,
+                                                 int32_t *selected_samples_idx,
+                                                 int32_t *n_selected_gt_threshold,
+                                                 int32_t *n_selected_eq_threshold,
+                                                 int64_t n_samples, int64_t work_group_size,
+                                                 kmc_stream_t stream);
+int kmc_select_samples_far_from_centroid_f32_i64(int64_t n_selected,
+                                                 const float *distance_to_centroid,
+                                                 const float *threshold,
+                                                 int64_t *selected_samples_idx,
+                                                 int64_t *n_selected_gt_threshold,
+                                                 int64_t *n_selected_eq_threshold,
+                                                 int64_t n_samples, int64_t work_group_size,
+                                                 kmc_stream_t stream);
+int kmc_select_samples_far_from_centroid_f64_i32(int64_t n_selected,
+                                                 const double *distance_to_centroid,
+                                                 const double *threshold,
+                                                 int32_t *selected_samples_idx,
+                                                 int32_t *n_selected_gt_threshold,
+                                                 int32_t *n_selected_eq_threshold,
+                                                 int64_t n_samples, int64_t work_group_size,
+                                                 kmc_stream_t stream);
+int kmc_select_samples_far_from_centroid_f64_i64(int64_t n_selected,
+                                                 const double *distance_to_centroid,
+                                                 const double *threshold,
+                                                 int64_t *selected_samples_idx,
+                                                 int64_t *n_selected_gt_threshold,
+                                                 int64_t *n_selected_eq_threshold,
+                                                 int64_t n_samples, int64_t work_group_size,
+                                                 kmc_stream_t stream);
+
+/* ---- relocate_empty_clusters --------------------------------------------------
+ * replaces py_relocate_empty_clusters (_kmeans_lloyd.cpp:443-589) ->
+ * relocate_empty_clusters (src/util_kernels.hpp:392-476): threshold, select,
+ * relocate.  Empty cluster r (in list order) takes the r-th farthest sample by
+ * sq_dist_to_nearest_centroid (ties by lowest sample index). */
+int kmc_relocate_empty_clusters_f32_i32(int64_t n_empty_clusters, const float *X_t,
+                                        const float *sample_weights,
+                                        const int32_t *assignment_id,
+                                        const int32_t *empty_clusters_list,
+                                        const float *sq_dist_to_nearest_centroid,
+                                        float *centroid_t, float *cluster_sizes,
+                                        float *per_sample_inertia, int64_t n_samples,
+                                        int64_t n_features, int64_t n_clusters,
+                                        int64_t work_group_size, kmc_stream_t stream);
+int kmc_relocate_empty_clusters_f32_i64(int64_t n_empty_clusters, const float *X_t,
+                                        const float *sample_weights,
+                                        const int64_t *assignment_id,
+                                        const int64_t *empty_clusters_list,
+                                        const float *sq_dist_to_nearest_centroid,
+                                        float *centroid_t, float *cluster_sizes,
+                                        float *per_sample_inertia, int64_t n_samples,
+                                        int64_t n_features, int64_t n_clusters,
+                                        int64_t work_group_size, kmc_stream_t stream);
+int kmc_relocate_empty_clusters_f64_i32(int64_t n_empty_clusters, const double *X_t,
+                                        const double *sample_weights,
+                                        const int32_t *assignment_id,
+                                        const int32_t *empty_clusters_list,
+                                        const double *sq_dist_to_nearest_centroid,
+                                        double *centroid_t, double *cluster_sizes,
+                                        double *per_sample_inertia, int64_t n_samples,
+                                        int64_t n_features, int64_t n_clusters,
+                                        int64_t work_group_size, kmc_stream_t stream);
+int kmc_relocate_empty_clusters_f64_i64(int64_t n_empty_clusters, const double *X_t,
+                                        const double *sample_weights,
+                                        const int64_t *assignment_id,
+                                        const int64_t *empty_clusters_list,
+                                        const double *sq_dist_to_nearest_centroid,
+                                        double *centroid_t, double *cluster_sizes,
+                                        double *per_sample_inertia, int64_t n_samples,
+                                        int64_t n_features, int64_t n_clusters,
+                                        int64_t work_group_size, kmc_stream_t stream);
+
+/* ---- compute_centroid_shifts_squared: out[j] = sum_f (old[f,j]-new[f,j])^2 ---
+ * replaces py_compute_centroid_shifts_squared_kernel (_kmeans_lloyd.cpp:591-664)
+ * -> compute_centroid_shifts_squared_kernel (src/util_kernels.hpp:481-516). */
+int kmc_compute_centroid_shifts_squared_f32(const float *centroid_t,
+                                            const float *new_centroid_t,
+                                            float *out_centroid_shifts, int64_t n_features,
+                                            int64_t n_clusters, kmc_stream_t stream);
+int kmc_compute_centroid_shifts_squared_f64(const double *centroid_t,
+                                            const double *new_centroid_t,
+                                            double *out_centroid_shifts, int64_t n_features,
+                                            int64_t n_clusters, kmc_stream_t stream);
+
+/* ---- compute_centroid_to_sample_distances: (n_clusters, n_samples) ----------
+ * replaces py_compute_distances (_kmeans_lloyd.cpp:666-745) ->
+ * compute_distances (src/compute_euclidean_distance.hpp:12-114). */
+int kmc_compute_centroid_to_sample_distances_f32(const float *X_t, const float *centroid_t,
+                                                 float *euclidean_distances_t,
+                                                 int64_t n_samples, int64_t n_features,
+                                                 int64_t n_clusters, int64_t work_group_size,
+                                                 int64_t centroids_window_height,
+                                                 kmc_stream_t stream);
+int kmc_compute_centroid_to_sample_distances_f64(const double *X_t, const double *centroid_t,
+                                                 double *euclidean_distances_t,
+                                                 int64_t n_samples, int64_t n_features,
+                                                 int64_t n_clusters, int64_t work_group_size,
+                                                 int64_t centroids_window_height,
+                                                 kmc_stream_t stream);
+
+/* ---- assignment: labels of the nearest centroid -------------------------------
+ * replaces py_assignment (_kmeans_lloyd.cpp:747-839) -> assignment
+ * (src/assignment.hpp:11-146). */
+int kmc_assignment_f32_i32(const float *X_t, const float *centroids_t,
+                           const float *centroids_half_l2_norm, int32_t *assignment_id,
+                           int64_t n_samples, int64_t n_features, int64_t n_clusters,
+                           int64_t centroids_window_height, int64_t work_group_size,
+                           kmc_stream_t stream);
+int kmc_assignment_f32_i64(const float *X_t, const float *centroids_t,
+                           const float *centroids_half_l2_norm, int64_t *assignment_id,
+                           int64_t n_samples, int64_t n_features, int64_t n_clusters,
+                           int64_t centroids_window_height, int64_t work_group_size,
+                           kmc_stream_t stream);
+int kmc_assignment_f64_i32(const double *X_t, const double *centroids_t,
+                           const double *centroids_half_l2_norm, int32_t *assignment_id,
+                           int64_t n_samples, int64_t n_features, int64_t n_clusters,
+                           int64_t centroids_window_height, int64_t work_group_size,
+                           kmc_stream_t stream);
+int kmc_assignment_f64_i64(const double *X_t, const double *centroids_t,
+                           const double *centroids_half_l2_norm, int64_t *assignment_id,
+                           int64_t n_samples, int64_t n_features, int64_t n_clusters,
+                           int64_t centroids_window_height, int64_t work_group_size,
+                           kmc_stream_t stream);
+
+/* ---- compute_inertia: out[i] = w[i] * ||x_i - c_label(i)||^2 ----------------
+ * replaces py_compute_inertia (_kmeans_lloyd.cpp:841-939) ->
+ * compute_inertia_kernel (src/compute_inertia.hpp:11-53). */
+int kmc_compute_inertia_f32_i32(const float *X_t, const float *sample_weight,
+                                const float *centroid_t, const int32_t *assignment_id,
+                                float *per_sample_inertia, int64_t n_samples,
+                                int64_t n_features, int64_t n_clusters,
+                                int64_t work_group_size, kmc_stream_t stream);
+int kmc_compute_inertia_f32_i64(const float *X_t, const float *sample_weight,
+                                const float *centroid_t, const int64_t *assignment_id,
+                                float *per_sample_inertia, int64_t n_samples,
+                                int64_t n_features, int64_t n_clusters,
+                                int64_t work_group_size, kmc_stream_t stream);
+int kmc_compute_inertia_f64_i32(const double *X_t, const double *sample_weight,
+                                const double *centroid_t, const int32_t *assignment_id,
+                                double *per_sample_inertia, int64_t n_samples,
+                                int64_t n_features, int64_t n_clusters,
+                                int64_t work_group_size, kmc_stream_t stream);
+int kmc_compute_inertia_f64_i64(const double *X_t, const double *sample_weight,
+                                const double *centroid_t, const int64_t *assignment_id,
+                                double *per_sample_inertia, int64_t n_samples,
+                                int64_t n_features, int64_t n_clusters,
+                                int64_t work_group_size, kmc_stream_t stream);
+
+/* ---- reduce_vector_blocking: blocking sum of a vector ------------------------
+ * replaces py_reduce_vector_blocking (_kmeans_lloyd.cpp:941-976) ->
+ * reduce_vector_kernel_blocking (src/compute_inertia.hpp:104-135).
+ * The sum is accumulated in float64 and rounded once to dataT.  Blocks until
+ * the result is on the host. */
+int kmc_reduce_vector_blocking_f32(const float *data, int64_t n, kmc_stream_t stream,
+                                   float *result);
+int kmc_reduce_vector_blocking_f64(const double *data, int64_t n, kmc_stream_t stream,
+                                   double *result);
+
+/* ---- fused_lloyd_single_step ----------------------------------------------------
+ * replaces py_fused_lloyd_single_step (_kmeans_lloyd.cpp:980-1109) ->
+ * lloyd_single_step (src/lloyd_single_step.hpp:37-209).  Labels are written;
+ * w*x and w are ADDED into the caller-zeroed private copies. */
+int kmc_fused_lloyd_single_step_f32_i32(const float *X_t, const float *sample_weight,
+                                        const float *centroids_t,
+                                        const float *centroids_half_l2_norm,
+                                        int32_t *assignments_idx,
+                                        float *new_centroids_t_private_copies,
+                                        float *cluster_sizes_private_copies,
+                                        int64_t n_samples, int64_t n_features,
+                                        int64_t n_clusters, int64_t n_copies,
+                                        int64_t centroids_window_height,
+                                        int64_t work_group_size, kmc_stream_t stream);
+int kmc_fused_lloyd_single_step_f32_i64(const float *X_t, const float *sample_weight,
+                                        const float *centroids_t,
+                                        const float *centroids_half_l2_norm,
+                                        int64_t *assignments_idx,
+                                        float *new_centroids_t_private_copies,
+                                        float *cluster_sizes_private_copies,
+                                        int64_t n_samples, int64_t n_features,
+                                        int64_t n_clusters, int64_t n_copies,
+                                        int64_t centroids_window_height,
+                                        int64_t work_group_size, kmc_stream_t stream);
+int kmc_fused_lloyd_single_step_f64_i32(const double *X_t, const double *sample_weight,
+                                        const double *centroids_t,
+                                        const double *centroids_half_l2_norm,
+                                        int32_t *assignments_idx,
+                                        double *new_centroids_t_private_copies,
+                                        double *cluster_sizes_private_copies,
+                                        int64_t n_samples, int64_t n_features,
+                                        int64_t n_clusters, int64_t n_copies,
+                                        int64_t centroids_window_height,
+                                        int64_t work_group_size, kmc_stream_t stream);
+int kmc_fused_lloyd_single_step_f64_i64(const double *X_t, const double *sample_weight,
+                                        const double *centroids_t,
+                                        const double *centroids_half_l2_norm,
+                                        int64_t *assignments_idx,
+                                        double *new_centroids_t_private_copies,
+                                        double *cluster_sizes_private_copies,
+                                        int64_t n_samples, int64_t n_features,
+                                        int64_t n_clusters, int64_t n_copies,
+                                        int64_t centroids_window_height,
+                                        int64_t work_group_size, kmc_stream_t stream);
+
+/* ---- compute_number_of_private_copies ---------------------------------------------
+ * replaces py_compute_number_of_private_copies (_kmeans_lloyd.cpp:1111-1147) ->
+ * compute_number_of_private_copies (src/lloyd_single_step.hpp:12-35).
+ * element_size is sizeof(dataT); l2_cache_bytes <= 0 queries the current
+ * device.  Pure host arithmetic otherwise. */
+int kmc_compute_number_of_private_copies(int64_t element_size, int64_t n_samples,
+                                         int64_t n_features, int64_t n_clusters,
+                                         double centroids_private_copies_max_cache_occupancy,
+                                         int64_t work_group_size, int64_t l2_cache_bytes,
+                                         int64_t *n_copies_out);
+
+/* ---- kmeans_lloyd_driver -----------------------------------------------------------
+ * replaces py_kmeans_lloyd_driver (_kmeans_lloyd.cpp:1149-1275) -> driver_lloyd
+ * (src/kmeans_lloyd_driver.hpp:21-431).  Blocking.  init_centroids_t is
+ * overwritten (the two centroid buffers ping-pong).  The convergence sum and
+ * the returned inertia are accumulated in float64 and rounded to dataT.
+ * print_fn receives the verbose per-iteration lines (may be NULL). */
+typedef void (*kmc_print_fn)(const char *line, void *ctx);
+int kmc_lloyd_driver_f32_i32(const float *X_t, const float *sample_weight,
+                             float *init_centroids_t, int32_t *assignment_id,
+                             float *res_centroids_t, int64_t n_samples, int64_t n_features,
+                             int64_t n_clusters, double tol, int verbose, int64_t max_iter,
+                             int64_t centroids_window_height, int64_t work_group_size,
+                             double centroids_private_copies_max_cache_occupancy,
+                             kmc_stream_t stream, kmc_print_fn print_fn, void *print_ctx,
+                             int64_t *n_iters_out, float *total_inertia_out);
+int kmc_lloyd_driver_f32_i64(const float *X_t, const float *sample_weight,
+                             float *init_centroids_t, int64_t *assignment_id,
+                             float *res_centroids_t, int64_t n_samples, int64_t n_features,
+                             int64_t n_clusters, double tol, int verbose, int64_t max_iter,
+                             int64_t centroids_window_height, int64_t work_group_size,
+                             double centroids_private_copies_max_cache_occupancy,
+                             kmc_stream_t stream, kmc_print_fn print_fn, void *print_ctx,
+                             int64_t *n_iters_out, float *total_inertia_out);
+int kmc_lloyd_driver_f64_i32(const double *X_t, const double *sample_weight,
+                             double *init_centroids_t, int32_t *assignment_id,
+                             double *res_centroids_t, int64_t n_samples, int64_t n_features,
+                             int64_t n_clusters, double tol, int verbose, int64_t max_iter,
+                             int64_t centroids_window_height, int64_t work_group_size,
+                             double centroids_private_copies_max_cache_occupancy,
+                             kmc_stream_t stream, kmc_print_fn print_fn, void *print_ctx,
+                             int64_t *n_iters_out, double *total_inertia_out);
+int kmc_lloyd_driver_f64_i64(const double *X_t, const double *sample_weight,
+                             double *init_centroids_t, int64_t *assignment_id,
+                             double *res_centroids_t, int64_t n_samples, int64_t n_features,
+                             int64_t n_clusters, double tol, int verbose, int64_t max_iter,
+                             int64_t centroids_window_height, int64_t work_group_size,
+                             double centroids_private_copies_max_cache_occupancy,
+                             kmc_stream_t stream, kmc_print_fn print_fn, void *print_ctx,
+                             int64_t *n_iters_out, double *total_inertia_out);
+
+/* ---- fit sessions: the driver loop of driver_lloyd (src/kmeans_lloyd_driver.hpp:
+ * 83-354) as a resumable handle.  kmeans_lloyd_driver is create + run +
+ * finalize + destroy.  A session keeps data, centroids and loop state on the
+ * device; kmc_fit_step enqueues iterations without host synchronisation (the
+ * GPU stops the loop itself once tol or max_iter is reached).
+ * form: KMC_FORM_PLAIN (exact dataT arithmetic, the reference's) or a mixed
+ * tensor-core form (float32 data only). */
+typedef struct kmc_fit_s *kmc_fit_t;
+#define KMC_FORM_PLAIN 0
+#define KMC_FORM_MIXED_BF16 1
+#define KMC_FORM_MIXED_FP16 2
+int kmc_fit_create_f32_i32(const float *X_t, const float *sample_weight, float *centroids_t,
+                           int32_t *assignment_id, float *res_centroids_t, int64_t n_samples,
+                           int64_t n_features, int64_t n_clusters, double tol, int64_t max_iter,
+                           int form, kmc_stream_t stream, kmc_fit_t *fit_out);
+int kmc_fit_create_f32_i64(const float *X_t, const float *sample_weight, float *centroids_t,
+                           int64_t *assignment_id, float *res_centroids_t, int64_t n_samples,
+                           int64_t n_features, int64_t n_clusters, double tol, int64_t max_iter,
+                           int form, kmc_stream_t stream, kmc_fit_t *fit_out);
+int kmc_fit_create_f64_i32(const double *X_t, const double *sample_weight, double *centroids_t,
+                           int32_t *assignment_id, double *res_centroids_t, int64_t n_samples,
+                           int64_t n_features, int64_t n_clusters, double tol, int64_t max_iter,
+                           int form, kmc_stream_t stream, kmc_fit_t *fit_out);
+int kmc_fit_create_f64_i64(const double *X_t, const double *sample_weight, double *centroids_t,
+                           int64_t *assignment_id, double *res_centroids_t, int64_t n_samples,
+                           int64_t n_features, int64_t n_clusters, double tol, int64_t max_iter,
+                           int form, kmc_stream_t stream, kmc_fit_t *fit_out);
+/* Enqueue n_iterations iterations (asynchronous; no-ops once the loop stopped). */
+int kmc_fit_step(kmc_fit_t fit, int64_t n_iterations);
+/* Run to convergence (blocking). */
+int kmc_fit_run(kmc_fit_t fit);
+/* Blocking read of the loop state. */
+int kmc_fit_status(kmc_fit_t fit, int64_t *n_iter_out, int *done_out, double *last_shift_out);
+/* Final assignment + inertia against the current centroids (blocking). */
+int kmc_fit_finalize(kmc_fit_t fit, int64_t *n_iter_out, double *total_inertia_out);
+/* Per-phase CUDA-event timing (off by default): phase 0 is the assignment +
+ * accumulation kernel of every iteration.  Times are summed over recorded
+ * iterations; reading them synchronises the stream. */
+int kmc_fit_set_profiling(kmc_fit_t fit, int enable);
+int kmc_fit_phase_time(kmc_fit_t fit, int phase, double *total_ms_out, int64_t *count_out);
+/* Kernel launches enqueued so far by this session. */
+int kmc_fit_launch_count(kmc_fit_t fit, int64_t *launches_out);
+int kmc_fit_destroy(kmc_fit_t fit);
+
+/* ---- events: the (host_task_event, compute_event) pair of the reference ------------
+ * The reference returns sycl::event pairs from every wrapper
+ * (e.g. _kmeans_lloyd.cpp:102-103) and accepts `depends` lists.  These wrap
+ * cudaEvent_t so a host binding can offer the same .wait() / depends. */
+int kmc_event_create(kmc_event_t *event_out);
+int kmc_event_record(kmc_event_t event, kmc_stream_t stream);
+int kmc_event_synchronize(kmc_event_t event);
+int kmc_event_query(kmc_event_t event, int *completed_out);
+int kmc_stream_wait_event(kmc_stream_t stream, kmc_event_t event);
+int kmc_event_destroy(kmc_event_t event);
+int kmc_stream_synchronize(kmc_stream_t stream);
+/* Device ordinal owning a pointer (-1 for host memory); replaces the
+ * reference's queue-compatibility check (_kmeans_lloyd.cpp:46-56). */
+int kmc_pointer_device(const void *ptr, int *device_out);
+int kmc_current_device(int *device_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KMEANS_GB300_H */

@@ -1,0 +1,99 @@
+// Shared definitions for the GB300 Lloyd k-means engine (device + host side).
+//
+// Every kernel in this library follows the semantics of the SYCL kernels in
+// src/*.hpp of kmeans_dpcpp; the per-kernel files cite the exact lines.
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <cmath>
+#include <limits>
+#include <string>
+#include <cuda_runtime.h>
+
+#include "../../include/kmeans_gb300.h"
+
+namespace kmc {
+
+// ---------------------------------------------------------------------------
+// Error reporting.  The C-ABI never throws; every entry point returns a status
+// code and leaves a human-readable message in a thread-local buffer.
+// ---------------------------------------------------------------------------
+void set_error(const char *fmt, ...);
+const char *get_error();
+
+#define KMC_CUDA_TRY(...)                                                       \
+    do {                                                                        \
+        cudaError_t _e = (__VA_ARGS__);                                                \
+        if (_e != cudaSuccess) {                                                \
+            ::kmc::set_error("CUDA error %s (%d) at %s:%d: %s",                 \
+                             cudaGetErrorName(_e), (int)_e, __FILE__, __LINE__, \
+                             cudaGetErrorString(_e));                           \
+            return (_e == cudaErrorMemoryAllocation) ? KMC_ERR_OUT_OF_MEMORY    \
+                                                     : KMC_ERR_CUDA;            \
+        }                                                                       \
+    } while (0)
+
+#define KMC_TRY(...)                      \
+    do {                                  \
+        int _s = (__VA_ARGS__);           \
+        if (_s != KMC_OK) return _s;      \
+    } while (0)
+
+#define KMC_CHECK_ARG(cond, ...)                    \
+    do {                                            \
+        if (!(cond)) {                              \
+            ::kmc::set_error(__VA_ARGS__);          \
+            return KMC_ERR_INVALID_ARGUMENT;        \
+        }                                           \
+    } while (0)
+
+inline int check_launch(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("kernel launch failed (%s): %s", what, cudaGetErrorString(e));
+        return KMC_ERR_CUDA;
+    }
+    return KMC_OK;
+}
+
+// quotient_ceil of src/quotients_utils.hpp:5-6
+template <typename T>
+__host__ __device__ constexpr T ceil_div(T a, T b) { return (a + b - 1) / b; }
+
+template <typename T>
+__host__ __device__ inline T pos_inf() { return std::numeric_limits<T>::infinity(); }
+
+// Number of SMs of the current device (cached per device).
+int num_sms();
+// L2 size in bytes of the current device.
+int64_t l2_bytes();
+
+// Stream-ordered scratch allocation (cudaMallocAsync on the caller's stream).
+struct Scratch {
+    void *ptr = nullptr;
+    cudaStream_t stream = nullptr;
+    Scratch() = default;
+    Scratch(const Scratch &) = delete;
+    Scratch &operator=(const Scratch &) = delete;
+    int alloc(size_t bytes, cudaStream_t s) {
+        stream = s;
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMallocAsync(&ptr, bytes, s);
+        if (e != cudaSuccess) {
+            ptr = nullptr;
+            set_error("cudaMallocAsync(%zu) failed: %s", bytes, cudaGetErrorString(e));
+            return KMC_ERR_OUT_OF_MEMORY;
+        }
+        return KMC_OK;
+    }
+    ~Scratch() {
+        if (ptr) cudaFreeAsync(ptr, stream);
+    }
+    template <typename U> U *as() const { return static_cast<U *>(ptr); }
+};
+
+// Round a byte count up to a multiple of 256 (suballocation alignment).
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace kmc

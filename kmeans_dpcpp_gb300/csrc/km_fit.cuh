@@ -1,0 +1,93 @@
+// One Lloyd fit: workspace, iteration body and device-resident loop state.
+#pragma once
+
+#include <memory>
+#include <utility>
+#include <vector>
+
+#include "km_kernels.cuh"
+
+namespace kmc {
+
+template <typename T, typename I>
+struct FitParams {
+    const T *X = nullptr;         // (d, n) feature-major samples
+    const T *w = nullptr;         // (n,) sample weights
+    T *centroids = nullptr;       // (d, k) current centroids; overwritten
+    T *new_centroids = nullptr;   // (d, k) result buffer
+    I *labels = nullptr;          // (n,)
+    int64_t n = 0, d = 0, k = 0;
+    double tol = 0.0;
+    int64_t max_iter = 0;
+    int verbose = 0;
+    kmc_print_fn print_fn = nullptr;
+    void *print_ctx = nullptr;
+    cudaStream_t stream = nullptr;
+};
+
+struct FitBase {
+    // Optional CUDA-event timing of the assignment + accumulation phase.
+    bool profiling = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> phase_events;
+    int64_t launches = 0;
+
+    virtual ~FitBase() {
+        for (auto &e : phase_events) {
+            cudaEventDestroy(e.first);
+            cudaEventDestroy(e.second);
+        }
+    }
+    int phase_time(double *total_ms, int64_t *count) {
+        double tot = 0.0;
+        for (auto &e : phase_events) {
+            KMC_CUDA_TRY(cudaEventSynchronize(e.second));
+            float ms = 0.f;
+            KMC_CUDA_TRY(cudaEventElapsedTime(&ms, e.first, e.second));
+            tot += ms;
+        }
+        *total_ms = tot;
+        *count = (int64_t)phase_events.size();
+        return KMC_OK;
+    }
+    // Enqueue iterations until the loop stops (batches of at most max_batch
+    // iterations between host checks; <= 0 means unbounded growth).
+    virtual int run(int64_t max_batch) = 0;
+    // Enqueue exactly one iteration (no host synchronisation).
+    virtual int enqueue_iteration() = 0;
+    virtual int read_state(LoopState &out) = 0;
+    virtual int finalize(int64_t *n_iter_out, double *inertia_out) = 0;
+};
+
+template <typename T, typename I>
+struct PlainFit : FitBase {
+    FitParams<T, I> prm;
+    int64_t P = 1;  // private copies used internally
+    Scratch ws;
+    LoopState *state = nullptr;
+    T *hn = nullptr, *sizes = nullptr, *shifts = nullptr, *sq_dist = nullptr;
+    double *sums_cp = nullptr, *sizes_cp = nullptr;  // float64 accumulators
+    T *threshold = nullptr;
+    I *empty_list = nullptr, *n_empty = nullptr, *selected = nullptr, *counters = nullptr;
+    int64_t *gate = nullptr;
+    double *partials = nullptr, *dsum = nullptr;
+    void *thr_scratch = nullptr, *sel_scratch = nullptr;
+    int64_t issued = 0;
+    int host_done = 0;
+
+    int init(const FitParams<T, I> &p);
+    int enqueue_iteration() override;
+    int read_state(LoopState &out) override;
+    int run(int64_t max_batch) override;
+    int finalize(int64_t *n_iter_out, double *inertia_out) override;
+    // Assignment + accumulation of one iteration (the fused Lloyd step);
+    // reports the number of kernels it launched.
+    virtual int step_assign_and_accumulate(const T *cur, int64_t *n_launches);
+    // Labels against the final centroids (kmeans_lloyd_driver.hpp:372-386).
+    virtual int final_assignment();
+};
+
+// Mixed tensor-core form (kernels_mixed.cu); float32 data only.
+template <typename T, typename I>
+int make_mixed_fit(const FitParams<T, I> &p, int form, std::unique_ptr<FitBase> *out);
+
+}  // namespace kmc

@@ -1,0 +1,97 @@
+// Host-side launchers for every kernel of the engine.  Each launcher returns a
+// KMC_* status.  `guard`, when non-null, points to the device-resident loop
+// state of the Lloyd driver: guarded kernels return immediately once the loop
+// has stopped, so the driver can enqueue iterations ahead of the convergence
+// test without a host round-trip.
+#pragma once
+
+#include "km_common.cuh"
+
+namespace kmc {
+
+// Device-resident control block of one Lloyd fit (see driver.cu).
+struct LoopState {
+    int done;              // 1 once the loop stopped (max_iter or shift <= tol)
+    int relocations;       // number of iterations that relocated clusters
+    long long n_iter;      // iterations executed
+    long long max_iter;
+    double tol;            // tol rounded to dataT, widened back to double
+    double last_shift;     // float64 total of the last centroid shift
+    double last_inertia;   // float64 total of the verbose inertia (if computed)
+    unsigned int err;      // device-side error bits
+    unsigned int pad;
+};
+
+// ---- kernels_util.cu ----
+template <typename T>
+int launch_broadcast_divide(T *X, const T *y, int64_t rows, int64_t cols, cudaStream_t s);
+template <typename T>
+int launch_half_norm(const T *C, T *out, int64_t d, int64_t k, cudaStream_t s,
+                     const LoopState *guard = nullptr);
+// A: accumulator type of the private copies (dataT or double).
+template <typename T, typename I, typename A>
+int launch_reduce_centroids(const A *sizes_cp, const A *cent_cp, T *out_sizes, T *out_cent,
+                            I *empty_list, I *n_empty, int64_t P, int64_t d, int64_t k,
+                            cudaStream_t s, const LoopState *guard = nullptr);
+template <typename T>
+int launch_shifts(const T *old_c, const T *new_c, T *out, int64_t d, int64_t k,
+                  cudaStream_t s);
+// new_c /= sizes (per cluster), then shifts[j] = sum_f (old_c - new_c)^2.
+template <typename T>
+int launch_divide_and_shift(const T *old_c, T *new_c, const T *sizes, T *shifts, int64_t d,
+                            int64_t k, cudaStream_t s, const LoopState *guard);
+// Loop control: float64 total of shifts, n_iter += 1, convergence test.
+template <typename T>
+int launch_loop_control(const T *shifts, int64_t k, LoopState *state, cudaStream_t s);
+// w == nullptr selects the unit-weight variant.
+template <typename T, typename I>
+int launch_inertia(const T *X, const T *w, const T *C, const I *labels, T *out, int64_t n,
+                   int64_t d, int64_t k, cudaStream_t s, const LoopState *guard = nullptr,
+                   const int64_t *gate = nullptr);
+// Deterministic float64 sum of n values into *out (device).  `partials` must
+// hold sum_partials_size() doubles.
+int64_t sum_partials_size();
+template <typename T>
+int launch_sum_f64(const T *data, int64_t n, double *partials, double *out, cudaStream_t s,
+                   const LoopState *guard = nullptr);
+template <typename T>
+int launch_fill(T *p, T v, int64_t count, cudaStream_t s, const LoopState *guard = nullptr);
+
+// ---- kernels_lloyd.cu : SIMT tiled distance kernels (exact FP32/FP64) ----
+template <typename T, typename I>
+int launch_assignment(const T *X, const T *C, const T *hn, I *labels, int64_t n, int64_t d,
+                      int64_t k, cudaStream_t s, const LoopState *guard = nullptr);
+// A: accumulator type of the private copies (dataT for the public API,
+// double inside the driver so sums are rounded to dataT once).
+template <typename T, typename I, typename A>
+int launch_fused_step(const T *X, const T *w, const T *C, const T *hn, I *labels, A *sums_cp,
+                      A *sizes_cp, int64_t n, int64_t d, int64_t k, int64_t P, cudaStream_t s,
+                      const LoopState *guard = nullptr);
+template <typename T>
+int launch_distances(const T *X, const T *C, T *out, int64_t n, int64_t d, int64_t k,
+                     cudaStream_t s);
+
+// ---- kernels_reloc.cu : threshold (radix select), selection, relocation ----
+// Scratch bytes needed by launch_threshold for n samples.
+size_t threshold_scratch_bytes();
+template <typename T>
+int launch_threshold(const T *data, int64_t n, const int64_t *topk_dev, int64_t topk_host,
+                     T *threshold, void *scratch, cudaStream_t s,
+                     const LoopState *guard = nullptr);
+// Scratch for launch_select; max_selected bounds n_selected.
+size_t select_scratch_bytes(int64_t max_selected);
+template <typename T, typename I>
+int launch_select(const int64_t *n_selected_dev, int64_t n_selected_host, const T *dist,
+                  const T *threshold, I *selected, I *n_gt, I *n_eq, int64_t n, void *scratch,
+                  cudaStream_t s, const LoopState *guard = nullptr);
+template <typename T, typename I>
+int launch_relocate(const int64_t *n_empty_dev, int64_t n_empty_host, const T *X, const T *w,
+                    const I *labels, const I *selected, const I *n_gt, const I *empty_list,
+                    T *sums, T *sizes, T *inertia, int64_t n, int64_t d, int64_t k,
+                    cudaStream_t s, const LoopState *guard = nullptr);
+// Copies *n_empty (indT) into an int64 device scalar (0 when the loop stopped).
+template <typename I>
+int launch_gate_from_count(const I *n_empty, int64_t *gate, cudaStream_t s,
+                           const LoopState *guard);
+
+}  // namespace kmc
