@@ -20,7 +20,8 @@ def res(dt):
 def T(a, dtype=None):
     import torch
 
-    a = np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))
+    # np.array(copy=True, order="C") keeps 0-d arrays 0-d
+    a = np.array(a, dtype=dtype, copy=True, order="C")
     return torch.from_numpy(a).cuda()
 
 
@@ -77,7 +78,7 @@ def test_compute_threshold(golden, kdp, s, dt, topk, key):
     thr = T(np.full((), -127), dt)
     ht, _ = kdp.compute_threshold(data, topk, thr, sycl_queue=None)
     ht.wait()
-    assert float(H(thr)) == float(golden[f"threshold_{s}/{key}"])
+    assert H(thr).item() == float(golden[f"threshold_{s}/{key}"])
 
 
 @pytest.mark.parametrize("s,dt", DT)
@@ -97,7 +98,7 @@ def test_select_samples_far_from_centroid(golden, kdp, s, dt, it):
                                                   sycl_queue=None, depends=[c_ev])
     ht2.wait()
     ht.wait()
-    ng, nq, t = int(H(ngt)), int(H(neq)), float(H(thr))
+    ng, nq, t = H(ngt).item(), H(neq).item(), H(thr).item()
     s_np = H(sel)
     assert ng + nq - 1 == ne
     assert np.all(x[s_np[:ng]] > t)

@@ -19,7 +19,8 @@ RTOL_C = {np.float32: 1e-5, np.float64: 1e-12}
 def T(a, dtype=None):
     import torch
 
-    a = np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))
+    # np.array(copy=True, order="C") keeps 0-d arrays 0-d
+    a = np.array(a, dtype=dtype, copy=True, order="C")
     return torch.from_numpy(a).cuda()
 
 
@@ -130,12 +131,12 @@ def test_threshold_and_select_parity(kdp, oracle, dt, topk, ties):
     xg = T(x)
     thr = torch.empty((), dtype=xg.dtype, device="cuda")
     kdp.compute_threshold(xg, topk, thr, None)[0].wait()
-    assert float(H(thr)) == float(thr_o)
+    assert H(thr).item() == float(thr_o)
     sel = T(np.full(x.size, -5), np.int64)
     ngt, neq = T(np.zeros(()), np.int64), T(np.ones(()), np.int64)
     kdp.select_samples_far_from_centroid(topk, xg, thr, sel, ngt, neq, 256, None)[0].wait()
     sel_o, ng_o, nq_o = oracle.select_samples_far_from_centroid(topk, x, thr_o, fill=-5)
-    assert (int(H(ngt)), int(H(neq))) == (ng_o, nq_o)
+    assert (H(ngt).item(), H(neq).item()) == (ng_o, nq_o)
     np.testing.assert_array_equal(H(sel), sel_o)
 
 
@@ -214,8 +215,10 @@ def test_driver_edge_cases(kdp, oracle, n, d, k):
     it_g, lab_g, C_g, inr_g = _run_driver(kdp, X, C0, 0.0, 5, it=np.int64)
     assert it_g == it_o
     np.testing.assert_array_equal(lab_g, lab_o)
-    np.testing.assert_array_equal(np.isnan(C_g), np.isnan(C_o))
-    ok = ~np.isnan(C_o)
+    # clusters emptied by relocation divide a cancelled sum by zero: NaN or an
+    # inf whose sign depends on summation order -- only finite entries compare
+    np.testing.assert_array_equal(np.isfinite(C_g), np.isfinite(C_o))
+    ok = np.isfinite(C_o)
     np.testing.assert_allclose(C_g[ok], C_o[ok], rtol=1e-12)
 
 
