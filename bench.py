@@ -273,6 +273,94 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def _time_form(L, capi, Xg, wg, C0, n, d, k, form, steps, warmup, world, local, sample_clocks):
+    """Creates a fit session for `form` and times exactly `steps` iterations."""
+    import torch
+
+    stream = torch.cuda.Stream()
+    cur = torch.from_numpy(C0.copy()).cuda()
+    res_c = torch.empty_like(cur)
+    lab = torch.empty(n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    fit = ctypes.c_void_p()
+    c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    c0.record(stream)
+    capi.check(L.kmc_fit_create_f32_i32(Xg.data_ptr(), wg.data_ptr(), cur.data_ptr(), lab.data_ptr(),
+                                        res_c.data_ptr(), n, d, k, 0.0, warmup + steps + 1,
+                                        FORMS[form], stream.cuda_stream, ctypes.byref(fit)))
+    c1.record(stream)
+    c1.synchronize()
+    prep_ms = c0.elapsed_time(c1)
+    try:
+        capi.check(L.kmc_fit_set_profiling(fit, 1))
+        capi.check(L.kmc_fit_step(fit, warmup))
+        stream.synchronize()
+        ms0, n0, l0 = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+        capi.check(L.kmc_fit_phase_time(fit, 0, ctypes.byref(ms0), ctypes.byref(n0)))
+        capi.check(L.kmc_fit_launch_count(fit, ctypes.byref(l0)))
+        r0 = ctypes.c_int64()
+        capi.check(L.kmc_fit_rechecked(fit, None, ctypes.byref(r0), None))
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        uuid = None
+        try:
+            uuid = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
+        except Exception:
+            pass
+        barrier(world)
+        torch.cuda.synchronize()
+        with ClockSampler(uuid if sample_clocks else None) as clk:
+            if sample_clocks:
+                time.sleep(0.15)
+            ev0.record(stream)
+            capi.check(L.kmc_fit_step(fit, steps))
+            ev1.record(stream)
+            ev1.synchronize()
+            torch.cuda.synchronize()
+            barrier(world)
+            if sample_clocks:
+                time.sleep(0.05)
+        elapsed_ms = all_max(world, ev0.elapsed_time(ev1))
+        ms1, n1, l1 = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+        capi.check(L.kmc_fit_phase_time(fit, 0, ctypes.byref(ms1), ctypes.byref(n1)))
+        capi.check(L.kmc_fit_launch_count(fit, ctypes.byref(l1)))
+        r1, err = ctypes.c_int64(), ctypes.c_int()
+        capi.check(L.kmc_fit_rechecked(fit, None, ctypes.byref(r1), ctypes.byref(err)))
+        it, done, shift = ctypes.c_int64(), ctypes.c_int(), ctypes.c_double()
+        capi.check(L.kmc_fit_status(fit, ctypes.byref(it), ctypes.byref(done), ctypes.byref(shift)))
+    finally:
+        capi.check(L.kmc_fit_destroy(fit))
+    assert it.value == warmup + steps, (it.value, "the loop stopped early")
+    assert err.value == 0, "tensor-core kernel reported a device-side timeout"
+    kern_ms = (ms1.value - ms0.value) / max(1, n1.value - n0.value)
+    return {"value": world * steps / (elapsed_ms / 1000.0), "ms_per_step": elapsed_ms / steps,
+            "kernel_ms": kern_ms, "launches": int(l1.value - l0.value),
+            "rechecked_per_step": (r1.value - r0.value) / steps, "prep_ms": prep_ms,
+            "clocks": clk.summary() if sample_clocks else None}
+
+
+def _roofline(form, n, d, k, kern_ms, clocks, sm_count):
+    peaks, peak_src = measured_peaks()
+    flops = 2.0 * n * k * d
+    achieved = flops / (kern_ms * 1e-3) / 1e12
+    if form == "plain":
+        clk_mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
+        peak = sm_count * 128 * 2 * clk_mhz * 1e6 / 1e12
+        r = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+             "peak_source": f"nominal FP32 FFMA rate ({sm_count} SMs x 128 lanes x 2 flop x "
+                            f"{clk_mhz:.0f} MHz); the plain form runs on the FP32 pipe",
+             "kernel": "tile_kernel (exact fused assignment + accumulation)"}
+    else:
+        peak = peaks.get("bf16_tflops_sustained", 1700.0)
+        r = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+             "peak_source": f"bf16_tflops_sustained of MEASURED_PEAKS.json ({peak_src}); the "
+                            "fp16 dense tensor rate equals the bf16 one",
+             "kernel": "mixed_assign_kernel + recheck_kernel (tcgen05 assignment + accumulation)"}
+    r.update({"frac": achieved / peak, "traffic": None, "kernel_ms": kern_ms,
+              "flops_per_launch": flops,
+              "algorithmic_bytes_per_launch": n * d * (4 if form == "plain" else 2) + 4 * n})
+    return r
+
+
 def run_gb300(args, world, rank, local):
     import torch
 
@@ -284,83 +372,20 @@ def run_gb300(args, world, rank, local):
     w = WORKLOADS[args.workload]
     n, d, k = w["n"], w["d"], w["k"]
     X_t, C0 = workload_data(args.workload)
-    form_name = "plain" if args.form == "auto" else args.form
-    form = FORMS[form_name]
+    form = "mixed-fp16" if args.form == "auto" else args.form
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
 
-    # ---- device-resident timing through a fit session ----
-    stream = torch.cuda.Stream()
     Xg = torch.from_numpy(X_t).cuda()
     wg = torch.ones(n, dtype=torch.float32, device="cuda")
-    cur = torch.from_numpy(C0.copy()).cuda()
-    res_c = torch.empty_like(cur)
-    lab = torch.empty(n, dtype=torch.int32, device="cuda")
-    torch.cuda.synchronize()
-    fit = ctypes.c_void_p()
-    max_iter = args.warmup + args.steps + 1
-    capi.check(L.kmc_fit_create_f32_i32(Xg.data_ptr(), wg.data_ptr(), cur.data_ptr(), lab.data_ptr(),
-                                        res_c.data_ptr(), n, d, k, 0.0, max_iter, form,
-                                        stream.cuda_stream, ctypes.byref(fit)))
-    capi.check(L.kmc_fit_set_profiling(fit, 1))
-    capi.check(L.kmc_fit_step(fit, args.warmup))
-    stream.synchronize()
-    ms0, c0 = ctypes.c_double(), ctypes.c_int64()
-    capi.check(L.kmc_fit_phase_time(fit, 0, ctypes.byref(ms0), ctypes.byref(c0)))
-    l0 = ctypes.c_int64()
-    capi.check(L.kmc_fit_launch_count(fit, ctypes.byref(l0)))
-
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    uuid = None
-    try:
-        uuid = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
-    except Exception:
-        pass
-    barrier(world)
-    torch.cuda.synchronize()
-    with ClockSampler(uuid) as clk:
-        time.sleep(0.15)
-        ev0.record(stream)
-        capi.check(L.kmc_fit_step(fit, args.steps))
-        ev1.record(stream)
-        ev1.synchronize()
-        torch.cuda.synchronize()
-        barrier(world)
-        time.sleep(0.05)
-    elapsed_ms = ev0.elapsed_time(ev1)
-    elapsed_ms = all_max(world, elapsed_ms)
-    ms1, c1 = ctypes.c_double(), ctypes.c_int64()
-    capi.check(L.kmc_fit_phase_time(fit, 0, ctypes.byref(ms1), ctypes.byref(c1)))
-    l1 = ctypes.c_int64()
-    capi.check(L.kmc_fit_launch_count(fit, ctypes.byref(l1)))
-    it, done, shift = ctypes.c_int64(), ctypes.c_int(), ctypes.c_double()
-    capi.check(L.kmc_fit_status(fit, ctypes.byref(it), ctypes.byref(done), ctypes.byref(shift)))
-    capi.check(L.kmc_fit_destroy(fit))
-    assert it.value == args.warmup + args.steps, (it.value, "the loop stopped early")
-
-    ms_per_step = elapsed_ms / args.steps
-    value = world * args.steps / (elapsed_ms / 1000.0)
-
-    # ---- roofline of the dominant kernel ----
-    peaks, peak_src = measured_peaks()
-    kern_ms = (ms1.value - ms0.value) / max(1, c1.value - c0.value)
-    flops = 2.0 * n * k * d
-    if form_name == "plain":
-        sm_count = torch.cuda.get_device_properties(local).multi_processor_count
-        clk_mhz = clk.summary()["sm_max_mhz"] or 2070.0
-        peak_tf = sm_count * 128 * 2 * clk_mhz * 1e6 / 1e12
-        roofline = {"bound": "fp32", "achieved": flops / (kern_ms * 1e-3) / 1e12, "peak": peak_tf,
-                    "unit": "TFLOP/s", "traffic": None,
-                    "peak_source": f"nominal FP32 FFMA rate ({sm_count} SMs x 128 lanes x 2 flop "
-                                   f"x {clk_mhz:.0f} MHz); the plain form runs on the FP32 pipe",
-                    "kernel": "tile_kernel (fused assignment + accumulation)",
-                    "kernel_ms": kern_ms, "flops_per_launch": flops}
-    else:
-        peak_tf = peaks.get("bf16_tflops_sustained", 1700.0)
-        roofline = {"bound": "tensor", "achieved": flops / (kern_ms * 1e-3) / 1e12, "peak": peak_tf,
-                    "unit": "TFLOP/s", "traffic": None,
-                    "peak_source": f"bf16_tflops_sustained of {peak_src} MEASURED_PEAKS.json",
-                    "kernel": "mixed assignment + accumulation", "kernel_ms": kern_ms,
-                    "flops_per_launch": flops}
-    roofline["frac"] = roofline["achieved"] / roofline["peak"]
+    head = _time_form(L, capi, Xg, wg, C0, n, d, k, form, args.steps, args.warmup, world, local, True)
+    forms = {form: head}
+    if not args.no_compare:
+        for other in ("plain", "mixed-bf16", "mixed-fp16"):
+            if other not in forms:
+                st = min(args.steps, 10) if other == "plain" else args.steps
+                forms[other] = _time_form(L, capi, Xg, wg, C0, n, d, k, other, st, args.warmup, world,
+                                          local, False)
+    roofline = _roofline(form, n, d, k, head["kernel_ms"], head["clocks"], sm_count)
 
     # ---- end to end through the drop-in surface, host buffers ----
     e2e = None
@@ -372,9 +397,9 @@ def run_gb300(args, world, rank, local):
         Cres_h = torch.empty_like(C_h).pin_memory()
         Xd = torch.empty_like(Xg)
         wd = torch.empty_like(wg)
-        Cd = torch.empty_like(cur)
-        Crd = torch.empty_like(cur)
-        labd = torch.empty_like(lab)
+        Cd = torch.from_numpy(C0.copy()).cuda()
+        Crd = torch.empty_like(Cd)
+        labd = torch.empty(n, dtype=torch.int32, device="cuda")
         barrier(world)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -383,36 +408,38 @@ def run_gb300(args, world, rank, local):
         Cd.copy_(C_h, non_blocking=True)
         torch.cuda.current_stream().synchronize()
         n_iter, inertia = kdp.kmeans_lloyd_driver(Xd, wd, Cd, labd, Crd, 0.0, False, args.steps, 8, 128,
-                                                  0.7, None)
+                                                  0.7, None, form=form)
         lab_h.copy_(labd)
         Cres_h.copy_(Crd)
         torch.cuda.synchronize()
-        t_e2e = time.perf_counter() - t0
-        t_e2e = all_max(world, t_e2e)
+        t_e2e = all_max(world, time.perf_counter() - t0)
         assert n_iter == args.steps
         h2d = X_t.nbytes + 4 * n + C0.nbytes
         d2h = 4 * n + C0.nbytes + 4
         e2e = {"value": world * n_iter / t_e2e, "unit": "iter/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h,
-               "note": "one kmeans_lloyd_driver call of K iterations (tol=0) with pinned-host "
-                       "copies of X, weights, init centroids in and labels, centroids, inertia "
-                       "out; bytes are per call"}
+               "note": "one kmeans_lloyd_driver call (form=%s) of K iterations (tol=0): pinned-host "
+                       "copies of X, weights, init centroids in and labels, centroids, inertia out, "
+                       "plus the one-time operand conversion; bytes are per call" % form}
         del Xd, X_h
 
     line = {
-        "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32" if form_name == "plain" else form_name.split("-")[1],
+        "metric": METRIC, "value": head["value"], "unit": "iter/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if form == "plain" else form.split("-")[1],
         "data": "synthetic",
         "config": {"workload": args.workload, "desc": w["desc"], "n": n, "d": d, "k": k,
-                   "form": form_name, "parallelism": f"replicas{world}",
+                   "form": form, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (X is %.2f GB)" % (X_t.nbytes / 1e9)},
         "roofline": roofline,
-        "clocks": clk.summary(),
-        "gpu_launches": int(l1.value - l0.value),
+        "clocks": head["clocks"],
+        "gpu_launches": head["launches"],
         "e2e": e2e,
+        "forms": {f: {kk: v for kk, v in r.items() if kk != "clocks"} for f, r in forms.items()},
     }
+    if "plain" in forms and form != "plain":
+        line["speedup_vs_plain_fp32"] = head["value"] / forms["plain"]["value"]
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(X_t, C0, target_s=args.cpu_seconds)
     if rank == 0:
@@ -429,6 +456,8 @@ def main(argv=None):
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c3")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="time only the headline form (no plain / other mixed comparison)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args(argv)
     if args.warmup < 3:

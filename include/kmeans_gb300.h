@@ -413,6 +413,11 @@ int kmc_fit_finalize(kmc_fit_t fit, int64_t *n_iter_out, double *total_inertia_o
  * iterations; reading them synchronises the stream. */
 int kmc_fit_set_profiling(kmc_fit_t fit, int enable);
 int kmc_fit_phase_time(kmc_fit_t fit, int phase, double *total_ms_out, int64_t *count_out);
+/* Mixed forms: samples whose tensor-core margin did not certify their label
+ * and were re-evaluated in exact float32 (last pass and running total), and
+ * the device-side error flag of the tensor-core kernel (1 after a bounded
+ * wait timed out).  Plain form: zeros.  Blocking. */
+int kmc_fit_rechecked(kmc_fit_t fit, int64_t *last_out, int64_t *total_out, int *device_error_out);
 /* Kernel launches enqueued so far by this session. */
 int kmc_fit_launch_count(kmc_fit_t fit, int64_t *launches_out);
 int kmc_fit_destroy(kmc_fit_t fit);

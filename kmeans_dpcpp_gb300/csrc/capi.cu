@@ -410,6 +410,10 @@ int kmc_fit_phase_time(kmc_fit_t fit, int phase, double *total_ms, int64_t *coun
     KMC_CHECK_ARG(total_ms != nullptr && count != nullptr, "null output pointer");
     return fit->impl->phase_time(total_ms, count);
 }
+int kmc_fit_rechecked(kmc_fit_t fit, int64_t *last, int64_t *total, int *device_error) {
+    KMC_FIT_CHECK(fit);
+    return fit->impl->counters(last, total, device_error);
+}
 int kmc_fit_launch_count(kmc_fit_t fit, int64_t *out) {
     KMC_FIT_CHECK(fit);
     KMC_CHECK_ARG(out != nullptr, "null output pointer");

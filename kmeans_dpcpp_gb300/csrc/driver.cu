@@ -113,8 +113,7 @@ int PlainFit<T, I>::enqueue_iteration() {
         phase_events.emplace_back(e0, e1);
     }
     // kmeans_lloyd_driver.hpp:155-170
-    KMC_TRY(launch_reduce_centroids<T, I, double>(sizes_cp, sums_cp, sizes, nxt, empty_list,
-                                                  n_empty, P, d, k, s, state));
+    KMC_TRY(reduce_step(nxt));
     int64_t verbose_launches = 0;
     if (p.verbose) {
         // kmeans_lloyd_driver.hpp:179-197: inertia of the *undivided* sums.
@@ -208,6 +207,13 @@ int PlainFit<T, I>::finalize(int64_t *n_iter_out, double *inertia_out) {
     if (n_iter_out) *n_iter_out = h.n_iter;
     if (inertia_out) *inertia_out = tot;
     return KMC_OK;
+}
+
+template <typename T, typename I>
+int PlainFit<T, I>::reduce_step(T *nxt) {
+    const FitParams<T, I> &p = prm;
+    return launch_reduce_centroids<T, I, double>(sizes_cp, sums_cp, sizes, nxt, empty_list,
+                                                 n_empty, P, p.d, p.k, p.stream, state);
 }
 
 template <typename T, typename I>

@@ -1,12 +1,931 @@
-// Mixed-precision (tcgen05 tensor-core) form of the Lloyd step.
+// Mixed-precision Lloyd step on the sm_103a tensor cores (tcgen05 + TMEM).
+//
+// The assignment needs, for each sample x and centroid c_j, the reference's
+// pseudo-distance D_j = half_norm[j] - x.c_j (src/device_functions.hpp:
+// 106-162).  Here the contraction x.c_j runs on the tensor cores with fp16
+// (or bf16) operands and fp32 accumulation; the score s_j = x.c_j - hn_j is
+// formed in fp32 with the reference's exact half norms.  For every sample the
+// epilogue finds the best score M and an exact bound on the runner-up R
+// without sorting (see "runner-up" below).  A sample whose margin M - R
+// exceeds twice its error bound E_i is certified: no rounding of the
+// operands, of the tensor-core accumulation or of the reference's own fp32
+// evaluation can change its winner, so its label equals the reference's.
+// Every other sample is re-evaluated in exact fp32 reference arithmetic over
+// the few centroids that can still win (recheck kernel), so labels never
+// drift from the plain form.
+//
+// Error bound (unscaled units, u = 2^-11 for fp16, 2^-8 for bf16, operands
+// scaled by a global power of two sigma, eta = 2^-25 the fp16 subnormal
+// half-spacing, d features):
+//   E_i = ||x_i||_2 * Cmax * kappa + (eta/sigma)(1+u)(||x_i||_1 + C1max)
+//         + d (eta/sigma)^2 + 2^-23 * 1.01 * Hmax
+//   kappa = 2u + u^2 + 2^-16 + (d + 4) 2^-23
+// with Cmax = max_j ||c_j||_2, C1max = max_j ||c_j||_1, Hmax = max_j |hn_j|.
+// It covers operand rounding (2u + u^2 per product), tensor-core fp32
+// accumulation (<= 2^-17 relative, allowing truncation), the fp32 score
+// rounding, and the reference's sequential fp32 dot (d 2^-24) and final
+// subtraction.  All norms are rounded up.
+//
+// Runner-up without sorting: per sample, P1[s] = max over 32-column
+// sub-chunk s and P2[t] = max over columns j = t (mod 32).  Two distinct
+// columns in the same sub-chunk lie in different classes, so
+//   runner-up = max(second largest P1, second largest P2),
+// and the winner is (argmax P1) * 32 + argmax P2 whenever the maximum is
+// unique (otherwise the margin is zero and the sample is rechecked).
+//
+// Kernel roles (one CTA of 448 threads per SM, persistent over 128-sample
+// tiles):
+//   warp 0      bulk copies: the centroid image once, X tiles into a 4-stage ring
+//   warp 1      TMEM allocation; one thread issues tcgen05.mma (M=128, N=256,
+//               K=16) into two 256-column TMEM accumulators
+//   warps 2-9   epilogue: tcgen05.ld, scores, P1/P2, certification, labels
+//   warps 10-13 update: w*x of certified samples into the cluster sums
+//               (red.global.add.v4.f32, cluster-major layout)
+// Samples that fail certification are accumulated by the recheck kernel.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+
 #include "km_fit.cuh"
+#include "km_mixed.cuh"
 
 namespace kmc {
 
+namespace {
+
+using namespace tc;
+
+constexpr int kTileM = 128;
+constexpr int kChunkN = 256;
+constexpr int kMaxStages = 4;
+__host__ __device__ constexpr int stages_for(int nkb) { return nkb == 1 ? 4 : 2; }
+constexpr int kEpiWarps = 8;
+constexpr int kUpdWarps = 4;
+constexpr int kThreadsMixed = 32 * (2 + kEpiWarps + kUpdWarps);
+constexpr int kMaxKPad = 2048;  // sub-chunk masks are 32 bits per column half
+constexpr uint32_t kTileBytes = kTileM * 128;  // one 64-wide K block of a tile
+constexpr size_t kSmemLimit = 232448;
+
+struct MixedConsts {
+    float inv_s2;   // 1 / sigma^2
+    float alpha;    // E_i = nx_i * alpha + n1_i * beta1 + beta0
+    float beta1;
+    float beta0;
+    float sigma;
+    unsigned int xmax_bits;  // max |x| (fp32 bits)
+    int pad0, pad1;
+};
+
+struct MixedArgs {
+    const uint8_t *ximg;
+    const uint8_t *cimg;
+    const float *hn;
+    const float *nx;
+    const float *n1;
+    const MixedConsts *consts;
+    const float *X;
+    const float *w;
+    void *labels;
+    float *sums_km;
+    float *sizes;
+    uint4 *cand;
+    int *flagged;
+    int *n_flagged;
+    int *err_global;
+    const LoopState *guard;
+    int64_t n, d, k, k_pad, d4;
+    int update;
+    int label64;
+};
+
+struct SmemLayout {
+    size_t c, x, hn, xch, lab, bar, total;
+};
+
+__host__ __device__ inline SmemLayout smem_layout(int nkb, int64_t k_pad) {
+    SmemLayout L;
+    size_t off = 0;
+    L.c = off;
+    off += (size_t)nkb * k_pad * 128;
+    off = (off + 1023) & ~size_t(1023);
+    L.x = off;
+    off += (size_t)stages_for(nkb) * nkb * kTileBytes;
+    L.hn = off;
+    off += sizeof(float) * k_pad;
+    L.xch = off;
+    off += sizeof(float) * 2 * 2 * kTileM * 3;
+    L.lab = off;
+    off += sizeof(int) * 2 * kTileM;
+    off = (off + 15) & ~size_t(15);
+    L.bar = off;
+    off += 8 * 18 + 16;
+    L.total = off + 1024;  // slack for aligning the dynamic shared memory base
+    return L;
+}
+
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+__device__ __forceinline__ bool epi_any(bool v) {
+    // OR over the 256 epilogue threads (named barrier 1)
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "barrier.red.or.pred q, 1, 256, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v)
+        : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+template <int BF16, int NKB>
+__global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArgs a) {
+    constexpr int kStages = stages_for(NKB);
+    if (a.guard != nullptr && *reinterpret_cast<const volatile int *>(&a.guard->done)) return;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    // the 128-byte swizzle is a function of absolute shared-memory address
+    // bits, so every operand image starts on a 1024-byte boundary
+    uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int64_t k_pad = a.k_pad;
+    const int nch = (int)(k_pad / kChunkN);
+    const SmemLayout L = smem_layout(NKB, k_pad);
+    uint8_t *cimg_s = smem + L.c;
+    uint8_t *xring = smem + L.x;
+    float *hn_s = reinterpret_cast<float *>(smem + L.hn);
+    float *xch = reinterpret_cast<float *>(smem + L.xch);
+    int *lab_s = reinterpret_cast<int *>(smem + L.lab);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.bar);
+    uint64_t *full = bars, *empty = bars + 4, *tfull = bars + 8, *tempty = bars + 10;
+    uint64_t *ufull = bars + 12, *uempty = bars + 14, *cbar = bars + 16, *tdone = bars + 17;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 18);
+    volatile int *err = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t n = a.n, k = a.k;
+    const int64_t ntiles = ceil_div<int64_t>(n, kTileM);
+    const uint32_t cbytes = (uint32_t)(NKB * k_pad * 128);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 32 * kEpiWarps);
+            mbar_init(&ufull[b], kTileM);
+            mbar_init(&uempty[b], kTileM);
+        }
+        mbar_init(cbar, 1);
+        mbar_init(tdone, 1);
+        *err = 0;
+        fence_barrier_init();
+    }
+    for (int64_t j = threadIdx.x; j < k_pad; j += blockDim.x)
+        hn_s[j] = (j < k) ? a.hn[j] : pos_inf<float>();
+    if (warp == 1) {
+        tmem_alloc(tmem_slot, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const MixedConsts cst = *a.consts;
+
+    if (warp == 0) {
+        // ------------------------------ producer ------------------------------
+        if (lane == 0) {
+            mbar_arrive_expect_tx(cbar, cbytes);
+            for (uint32_t off = 0; off < cbytes; off += 32768u)
+                bulk_g2s(cimg_s + off, a.cimg + off, min(32768u, cbytes - off), cbar);
+            int s = 0;
+            uint32_t ph = 0;
+            int issued[kMaxStages] = {0, 0, 0, 0};
+            uint32_t last_ph[kMaxStages] = {0, 0, 0, 0};
+            for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+                if (!mbar_wait(&empty[s], ph ^ 1u, err)) break;
+                mbar_arrive_expect_tx(&full[s], NKB * kTileBytes);
+                bulk_g2s(xring + (size_t)s * NKB * kTileBytes,
+                         a.ximg + (size_t)tile * NKB * kTileBytes, NKB * kTileBytes, &full[s]);
+                issued[s] = 1;
+                last_ph[s] = ph;
+                if (++s == kStages) {
+                    s = 0;
+                    ph ^= 1u;
+                }
+            }
+            // never leave a copy in flight into this CTA's shared memory
+            mbar_wait(cbar, 0, err);
+            for (int q = 0; q < kStages; ++q)
+                if (issued[q]) mbar_wait(&full[q], last_ph[q], err);
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ------------------------------ MMA issuer ----------------------------
+        if (lane == 0) {
+            const uint32_t idesc = idesc_f16(BF16, kTileM, kChunkN);
+            const uint32_t cbase = smem_u32(cimg_s);
+            bool ok = mbar_wait(cbar, 0, err);
+            int s = 0;
+            uint32_t ph = 0, cnt = 0;
+            for (int64_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+                if (!mbar_wait(&full[s], ph, err)) break;
+                tc_fence_after();
+                const uint32_t xbase = smem_u32(xring + (size_t)s * NKB * kTileBytes);
+                for (int c = 0; c < nch; ++c) {
+                    const uint32_t b = cnt & 1u, bph = (cnt >> 1) & 1u;
+                    if (!mbar_wait(&tempty[b], bph ^ 1u, err)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t dt = tmem + b * kChunkN;
+#pragma unroll
+                    for (int kb = 0; kb < NKB; ++kb)
+#pragma unroll
+                        for (int kk = 0; kk < 4; ++kk) {
+                            const uint64_t ad = desc_sw128(xbase + kb * kTileBytes + kk * 32);
+                            const uint64_t bd = desc_sw128(cbase + (uint32_t)(kb * k_pad * 128) +
+                                                           (uint32_t)(c * kChunkN * 128) + kk * 32);
+                            mma_f16(dt, ad, bd, idesc, (kb | kk) != 0 ? 1u : 0u);
+                        }
+                    mma_commit(&tfull[b]);
+                    ++cnt;
+                }
+                mma_commit(&empty[s]);
+                if (++s == kStages) {
+                    s = 0;
+                    ph ^= 1u;
+                }
+            }
+            // all issued MMAs must have finished before TMEM is released
+            mma_commit(tdone);
+            mbar_wait(tdone, 0, err);
+        }
+        __syncwarp();
+    } else if (warp < 2 + kEpiWarps) {
+        // ------------------------------ epilogue ------------------------------
+        const int ew = warp - 2;
+        const int q = warp & 3;   // TMEM lane quadrant accessible to this warp
+        const int h = ew >> 2;    // column half of each 256-wide chunk
+        const int row = 32 * q + lane;
+        const uint32_t lane_addr = (uint32_t)(32 * q) << 16;
+        uint32_t cnt = 0;
+        int tl = 0;
+        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tl) {
+            const int64_t i = tile * kTileM + row;
+            float E2 = 0.f;
+            if (i < n) {
+                float e = fmaf(a.nx[i], cst.alpha, fmaf(a.n1[i], cst.beta1, cst.beta0));
+                E2 = 2.f * e * 1.000001f;
+            }
+            float P2[32];
+#pragma unroll
+            for (int t = 0; t < 32; ++t) P2[t] = -pos_inf<float>();
+            float Mrun = -pos_inf<float>(), R1 = -pos_inf<float>();
+            int srun = 0;
+            uint32_t hot1 = 0u;
+            bool bad = false;
+            for (int c = 0; c < nch; ++c) {
+                const uint32_t b = cnt & 1u, bph = (cnt >> 1) & 1u;
+                if (!mbar_wait(&tfull[b], bph, err)) bad = true;
+                // tcgen05.ld is warp-collective: re-converge after the spin-wait
+                if (__any_sync(0xffffffffu, bad)) {
+                    bad = true;
+                    break;
+                }
+                tc_fence_after();
+#pragma unroll 1
+                for (int qq = 0; qq < 4; ++qq) {
+                    uint32_t r[32];
+                    tmem_ld32(tmem + lane_addr + b * kChunkN + h * 128 + qq * 32, r);
+                    tmem_ld_wait();
+                    const int j0 = c * kChunkN + h * 128 + qq * 32;
+                    const float4 *hv = reinterpret_cast<const float4 *>(hn_s + j0);
+                    float v[32];
+#pragma unroll
+                    for (int t4 = 0; t4 < 8; ++t4) {
+                        const float4 hh = hv[t4];
+                        v[4 * t4 + 0] = fmaf(__uint_as_float(r[4 * t4 + 0]), cst.inv_s2, -hh.x);
+                        v[4 * t4 + 1] = fmaf(__uint_as_float(r[4 * t4 + 1]), cst.inv_s2, -hh.y);
+                        v[4 * t4 + 2] = fmaf(__uint_as_float(r[4 * t4 + 2]), cst.inv_s2, -hh.z);
+                        v[4 * t4 + 3] = fmaf(__uint_as_float(r[4 * t4 + 3]), cst.inv_s2, -hh.w);
+                    }
+#pragma unroll
+                    for (int t = 0; t < 32; ++t) P2[t] = fmaxf(P2[t], v[t]);
+                    // sub-chunk maximum: ternary tree
+                    float m11[11];
+#pragma unroll
+                    for (int u = 0; u < 10; ++u) m11[u] = max3f(v[3 * u], v[3 * u + 1], v[3 * u + 2]);
+                    m11[10] = fmaxf(v[30], v[31]);
+                    const float m4a = max3f(m11[0], m11[1], m11[2]);
+                    const float m4b = max3f(m11[3], m11[4], m11[5]);
+                    const float m4c = max3f(m11[6], m11[7], m11[8]);
+                    const float m4d = fmaxf(m11[9], m11[10]);
+                    const float m = fmaxf(max3f(m4a, m4b, m4c), m4d);
+                    const int sidx = c * 4 + qq;
+                    if (m > Mrun) {
+                        R1 = Mrun;
+                        Mrun = m;
+                        srun = sidx;
+                    } else if (m > R1) {
+                        R1 = m;
+                    }
+                    // superset of the final hot sub-chunks: the final threshold
+                    // M - 2E is at least Mrun - 2E
+                    if (m >= Mrun - E2) hot1 |= 1u << sidx;
+                }
+                tc_fence_before();
+                mbar_arrive(&tempty[b]);
+                ++cnt;
+            }
+            if (epi_any(bad || *err != 0)) break;
+
+            // winner and runner-up within this column half
+            float M2 = -pos_inf<float>(), R2 = -pos_inf<float>();
+            int t2 = 0;
+#pragma unroll
+            for (int t = 0; t < 32; ++t) {
+                if (P2[t] > M2) {
+                    R2 = M2;
+                    M2 = P2[t];
+                    t2 = t;
+                } else if (P2[t] > R2) {
+                    R2 = P2[t];
+                }
+            }
+            const float Mh = Mrun;
+            const float Rh = fmaxf(R1, R2);
+            const int jh = (srun >> 2) * kChunkN + h * 128 + (srun & 3) * 32 + t2;
+            float *xb = xch + (size_t)(tl & 1) * (2 * kTileM * 3);
+            xb[(h * kTileM + row) * 3 + 0] = Mh;
+            xb[(h * kTileM + row) * 3 + 1] = __int_as_float(jh);
+            xb[(h * kTileM + row) * 3 + 2] = Rh;
+            epi_sync();
+            const float Mo = xb[((h ^ 1) * kTileM + row) * 3 + 0];
+            const int jo = __float_as_int(xb[((h ^ 1) * kTileM + row) * 3 + 1]);
+            const float Ro = xb[((h ^ 1) * kTileM + row) * 3 + 2];
+            float M, R;
+            int jw;
+            if (Mh > Mo) {
+                M = Mh;
+                jw = jh;
+                R = fmaxf(Rh, Mo);
+            } else if (Mo > Mh) {
+                M = Mo;
+                jw = jo;
+                R = fmaxf(Ro, Mh);
+            } else {
+                M = Mh;
+                jw = (h == 0) ? jh : jo;
+                R = Mh;  // tie (or both -inf): not certified
+            }
+            const bool cert = (M - R) > E2;  // false for NaN / infinities
+            if (i < n) {
+                if (!cert) {
+                    const float thr = M - E2;
+                    uint32_t hot2 = 0u;
+#pragma unroll
+                    for (int t = 0; t < 32; ++t)
+                        if (P2[t] >= thr) hot2 |= 1u << t;
+                    uint32_t *cw = reinterpret_cast<uint32_t *>(a.cand + i);
+                    cw[h] = hot1;
+                    cw[2 + h] = hot2;
+                    if (h == 0) {
+                        int pos = atomicAdd(a.n_flagged, 1);
+                        if (pos >= 0 && pos < n) a.flagged[pos] = (int)i;
+                    }
+                } else if (h == 0) {
+                    if (a.label64)
+                        reinterpret_cast<int64_t *>(a.labels)[i] = jw;
+                    else
+                        reinterpret_cast<int32_t *>(a.labels)[i] = jw;
+                }
+            }
+            if (a.update && h == 0) {
+                const int tb = tl & 1;
+                if (!mbar_wait(&uempty[tb], (((uint32_t)tl >> 1) & 1u) ^ 1u, err)) bad = true;
+                lab_s[tb * kTileM + row] = (cert && i < n) ? jw : -1;
+                mbar_arrive(&ufull[tb]);
+            }
+            if (epi_any(bad)) break;
+        }
+    } else {
+        // ------------------------------ update --------------------------------
+        if (a.update) {
+            const int row = threadIdx.x - 32 * (2 + kEpiWarps);
+            const int64_t d = a.d, d4 = a.d4;
+            int tl = 0;
+            for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tl) {
+                const int tb = tl & 1;
+                if (!mbar_wait(&ufull[tb], ((uint32_t)tl >> 1) & 1u, err)) break;
+                const int lab = lab_s[tb * kTileM + row];
+                mbar_arrive(&uempty[tb]);
+                const int64_t i = tile * kTileM + row;
+                if (lab >= 0 && lab < k && i < n) {
+                    const float wv = a.w[i];
+                    float4 *dst = reinterpret_cast<float4 *>(a.sums_km + (int64_t)lab * d4);
+                    for (int64_t g = 0; g < d4 / 4; ++g) {
+                        const int64_t f = 4 * g;
+                        float4 v;
+                        v.x = (f + 0 < d) ? __fmul_rn(a.X[(f + 0) * n + i], wv) : 0.f;
+                        v.y = (f + 1 < d) ? __fmul_rn(a.X[(f + 1) * n + i], wv) : 0.f;
+                        v.z = (f + 2 < d) ? __fmul_rn(a.X[(f + 2) * n + i], wv) : 0.f;
+                        v.w = (f + 3 < d) ? __fmul_rn(a.X[(f + 3) * n + i], wv) : 0.f;
+                        atomicAdd(dst + g, v);
+                    }
+                    atomicAdd(a.sizes + lab, wv);
+                }
+            }
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 512);
+    }
+    if (threadIdx.x == 0 && *err) atomicExch(a.err_global, 1);
+}
+
+// ---------------------------------------------------------------------------
+// preparation kernels
+// ---------------------------------------------------------------------------
+__global__ void absmax_kernel(const float *X, int64_t count, unsigned int *out_bits) {
+    float m = 0.f;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count;
+         e += (int64_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(X[e]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m == m) atomicMax(out_bits, __float_as_uint(m));
+}
+
+// sigma = 2^-e keeps the largest |x * sigma| at or below 2^14 (fp16 range);
+// bf16 shares fp32's exponent range and is never scaled.
+__global__ void sigma_kernel(MixedConsts *c, int bf16) {
+    float xmax = __uint_as_float(c->xmax_bits);
+    float sigma = 1.f;
+    if (!bf16) {
+        while (xmax * sigma > 16384.f && sigma > 1e-30f) sigma *= 0.5f;
+    }
+    c->sigma = sigma;
+    c->inv_s2 = 1.f / (sigma * sigma);
+}
+
+template <int BF16>
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+    if (BF16) {
+        __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&h);
+    } else {
+        __half2 h = __floats2half2_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&h);
+    }
+}
+
+// One thread per sample row (including the zero rows that pad the last
+// tile): the 128-byte-swizzled K-major image of (x * sigma), and the norms
+// ||x||_2, ||x||_1 rounded up.
+template <int BF16>
+__global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int nkb, int64_t rows,
+                               const MixedConsts *c, uint8_t *img, float *nx, float *n1) {
+    const float sigma = c->sigma;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t tile = i / kTileM;
+        const uint32_t r = (uint32_t)(i % kTileM);
+        double s2 = 0.0, s1 = 0.0;
+        for (int kb = 0; kb < nkb; ++kb) {
+            uint8_t *base = img + ((size_t)tile * nkb + kb) * kTileBytes;
+            for (int ch = 0; ch < 8; ++ch) {
+                float v[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int64_t f = (int64_t)kb * 64 + ch * 8 + e;
+                    const float x = (i < n && f < d) ? X[f * n + i] : 0.f;
+                    s2 += (double)x * (double)x;
+                    s1 += fabs((double)x);
+                    v[e] = x * sigma;
+                }
+                uint4 pk;
+                pk.x = pack2<BF16>(v[0], v[1]);
+                pk.y = pack2<BF16>(v[2], v[3]);
+                pk.z = pack2<BF16>(v[4], v[5]);
+                pk.w = pack2<BF16>(v[6], v[7]);
+                *reinterpret_cast<uint4 *>(base + sw128_offset(r, (uint32_t)ch * 8)) = pk;
+            }
+        }
+        if (i < n) {
+            nx[i] = __double2float_ru(sqrt(s2) * (1.0 + 1e-12));
+            n1[i] = __double2float_ru(s1 * (1.0 + 1e-12));
+        }
+    }
+}
+
+// Centroid image (rows j < k_pad, zero padding) and per-centroid norms.
+template <int BF16>
+__global__ void c_image_kernel(const float *C, int64_t d, int64_t k, int64_t k_pad, int nkb,
+                               const MixedConsts *c, uint8_t *img, float *cn2, float *cn1,
+                               const LoopState *guard) {
+    if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
+    const float sigma = c->sigma;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < k_pad;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        double s2 = 0.0, s1 = 0.0;
+        for (int kb = 0; kb < nkb; ++kb) {
+            uint8_t *base = img + (size_t)kb * k_pad * 128;
+            for (int ch = 0; ch < 8; ++ch) {
+                float v[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int64_t f = (int64_t)kb * 64 + ch * 8 + e;
+                    const float x = (j < k && f < d) ? C[f * k + j] : 0.f;
+                    s2 += (double)x * (double)x;
+                    s1 += fabs((double)x);
+                    v[e] = x * sigma;
+                }
+                uint4 pk;
+                pk.x = pack2<BF16>(v[0], v[1]);
+                pk.y = pack2<BF16>(v[2], v[3]);
+                pk.z = pack2<BF16>(v[4], v[5]);
+                pk.w = pack2<BF16>(v[6], v[7]);
+                *reinterpret_cast<uint4 *>(base + sw128_offset((uint32_t)j, (uint32_t)ch * 8)) = pk;
+            }
+        }
+        if (j < k) {
+            cn2[j] = __double2float_ru(sqrt(s2) * (1.0 + 1e-12));
+            cn1[j] = __double2float_ru(s1 * (1.0 + 1e-12));
+        }
+    }
+}
+
+// Per-iteration bound constants (one block).
+__global__ void bound_kernel(const float *cn2, const float *cn1, const float *hn, int64_t d,
+                             int64_t k, int bf16, MixedConsts *c, const LoopState *guard) {
+    if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
+    __shared__ float sh[3][32];
+    float m2 = 0.f, m1 = 0.f, mh = 0.f;
+    for (int64_t j = threadIdx.x; j < k; j += blockDim.x) {
+        m2 = fmaxf(m2, cn2[j]);
+        m1 = fmaxf(m1, cn1[j]);
+        mh = fmaxf(mh, fabsf(hn[j]));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+        m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+        mh = fmaxf(mh, __shfl_xor_sync(0xffffffffu, mh, o));
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        sh[0][wid] = m2;
+        sh[1][wid] = m1;
+        sh[2][wid] = mh;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            m2 = fmaxf(m2, sh[0][w]);
+            m1 = fmaxf(m1, sh[1][w]);
+            mh = fmaxf(mh, sh[2][w]);
+        }
+        m2 = fmaxf(m2, sh[0][0]);
+        m1 = fmaxf(m1, sh[1][0]);
+        mh = fmaxf(mh, sh[2][0]);
+        const double u = bf16 ? 0x1p-8 : 0x1p-11;
+        const double eta = (bf16 ? 0x1p-134 : 0x1p-25) / (double)c->sigma;
+        const double kappa = 2 * u + u * u + 0x1p-16 + (double)(d + 4) * 0x1p-23;
+        const double alpha = (double)m2 * kappa;
+        const double beta1 = eta * (1 + u);
+        const double beta0 = beta1 * (double)m1 + (double)d * eta * eta + 0x1p-23 * 1.01 * mh;
+        c->alpha = __double2float_ru(alpha * (1 + 1e-6));
+        c->beta1 = __double2float_ru(beta1 * (1 + 1e-6));
+        c->beta0 = __double2float_ru(beta0 * (1 + 1e-6) + 1e-37);
+    }
+}
+
+// Exact fp32 re-evaluation of samples whose margin did not certify them: the
+// reference's arithmetic (sequential fma dot, hn - dot, strict < in
+// ascending centroid order) over the candidate set, one warp per sample.
+__global__ void recheck_kernel(const float *X, const float *w, const float *C, const float *hn,
+                               const uint4 *cand, const int *flagged, const int *n_flagged,
+                               int64_t n, int64_t d, int64_t k, int64_t d4, void *labels,
+                               int label64, float *sums_km, float *sizes, int update,
+                               const LoopState *guard) {
+    if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
+    extern __shared__ float xs[];  // [warps][d]
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    float *x = xs + (size_t)wib * d;
+    const int64_t nf = (int64_t)*n_flagged;
+    const int64_t total = nf < n ? nf : n;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t e = blockIdx.x * (int64_t)(blockDim.x >> 5) + wib; e < total; e += nwarps) {
+        const int64_t i = flagged[e];
+        if (i < 0 || i >= n) continue;
+        for (int64_t f = lane; f < d; f += 32) x[f] = X[f * n + i];
+        __syncwarp();
+        const uint4 cm = cand[i];
+        const uint32_t h1[2] = {cm.x, cm.y}, h2[2] = {cm.z, cm.w};
+        float best = pos_inf<float>();
+        int bj = 0;
+        int idx = 0;
+        for (int h = 0; h < 2; ++h) {
+            for (uint32_t m1 = h1[h]; m1 != 0u; m1 &= m1 - 1u) {
+                const int s = __ffs(m1) - 1;
+                for (uint32_t m2 = h2[h]; m2 != 0u; m2 &= m2 - 1u, ++idx) {
+                    if ((idx & 31) != lane) continue;
+                    const int t = __ffs(m2) - 1;
+                    const int64_t j = (int64_t)(s >> 2) * kChunkN + h * 128 + (s & 3) * 32 + t;
+                    if (j >= k) continue;
+                    float dot = 0.f;
+                    for (int64_t f = 0; f < d; ++f) dot = __fmaf_rn(x[f], C[f * k + j], dot);
+                    const float D = hn[j] - dot;
+                    if (D < best || (D == best && j < bj)) {
+                        best = D;
+                        bj = (int)j;
+                    }
+                }
+            }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+            const int oj = __shfl_xor_sync(0xffffffffu, bj, off);
+            if (ob < best || (ob == best && oj < bj)) {
+                best = ob;
+                bj = oj;
+            }
+        }
+        if (lane == 0) {
+            if (label64)
+                reinterpret_cast<int64_t *>(labels)[i] = bj;
+            else
+                reinterpret_cast<int32_t *>(labels)[i] = bj;
+        }
+        if (update) {
+            const float wv = w[i];
+            for (int64_t f = lane; f < d; f += 32)
+                atomicAdd(sums_km + (int64_t)bj * d4 + f, __fmul_rn(x[f], wv));
+            if (lane == 0) atomicAdd(sizes + bj, wv);
+        }
+        __syncwarp();
+    }
+}
+
+// Cluster-major fp32 sums -> (d, k) centroid sums and sizes in dataT.
+__global__ void km_to_dk_kernel(const float *sums_km, const float *sizes32, float *out_c,
+                                float *out_sizes, int64_t d, int64_t k, int64_t d4,
+                                const LoopState *guard) {
+    if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < d * k + k;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        if (e < d * k) {
+            const int64_t f = e / k, j = e % k;
+            out_c[e] = sums_km[j * d4 + f];
+        } else {
+            out_sizes[e - d * k] = sizes32[e - d * k];
+        }
+    }
+}
+
+__global__ void reset_kernel(float *sums_km, int64_t count, float *sizes, int64_t k_pad,
+                             int *n_flagged, const LoopState *guard) {
+    if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count + k_pad;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        if (e < count)
+            sums_km[e] = 0.f;
+        else
+            sizes[e - count] = 0.f;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *n_flagged = 0;
+}
+
+// Copies the flagged count of this pass into the per-fit statistics.
+__global__ void stats_kernel(const int *n_flagged, long long *last, long long *total,
+                             const LoopState *guard) {
+    if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
+    *last = *n_flagged;
+    *total += *n_flagged;
+}
+
+unsigned grid1d(int64_t work, int block, int cap = 8192) {
+    int64_t g = ceil_div<int64_t>(work, block);
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, cap));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+template <typename I>
+struct MixedFit : PlainFit<float, I> {
+    using Base = PlainFit<float, I>;
+    int bf16 = 0;
+    int nkb = 1;
+    int64_t k_pad = 0, d4 = 0, ntiles = 0;
+    Scratch mws;
+    uint8_t *ximg = nullptr, *cimg = nullptr;
+    float *nx = nullptr, *n1 = nullptr, *sums_km = nullptr, *sizes32 = nullptr;
+    float *cn2 = nullptr, *cn1 = nullptr;
+    MixedConsts *consts = nullptr;
+    uint4 *cand = nullptr;
+    int *flagged = nullptr, *n_flagged = nullptr, *err_dev = nullptr;
+    long long *stats = nullptr;  // [0] last pass, [1] total
+
+    static bool supported(int64_t d, int64_t k) {
+        const int nk = (int)ceil_div<int64_t>(std::max<int64_t>(d, 1), 64);
+        const int64_t kp = ceil_div<int64_t>(std::max<int64_t>(k, 1), kChunkN) * kChunkN;
+        if (nk > 2 || kp > kMaxKPad) return false;
+        return smem_layout(nk, kp).total <= kSmemLimit;
+    }
+
+    int init_mixed(int form) {
+        const FitParams<float, I> &p = this->prm;
+        cudaStream_t s = p.stream;
+        bf16 = (form == KMC_FORM_MIXED_BF16) ? 1 : 0;
+        nkb = (int)ceil_div<int64_t>(std::max<int64_t>(p.d, 1), 64);
+        k_pad = ceil_div<int64_t>(p.k, kChunkN) * kChunkN;
+        d4 = ceil_div<int64_t>(std::max<int64_t>(p.d, 1), 4) * 4;
+        ntiles = ceil_div<int64_t>(p.n, kTileM);
+        size_t off = 0;
+        auto take = [&](size_t bytes) {
+            size_t o = off;
+            off += align256(bytes);
+            return o;
+        };
+        const size_t o_x = take((size_t)std::max<int64_t>(ntiles, 1) * nkb * kTileBytes);
+        const size_t o_c = take((size_t)nkb * k_pad * 128);
+        const size_t o_nx = take(sizeof(float) * p.n);
+        const size_t o_n1 = take(sizeof(float) * p.n);
+        const size_t o_skm = take(sizeof(float) * k_pad * d4);
+        const size_t o_s32 = take(sizeof(float) * k_pad);
+        const size_t o_cn2 = take(sizeof(float) * p.k);
+        const size_t o_cn1 = take(sizeof(float) * p.k);
+        const size_t o_cst = take(sizeof(MixedConsts));
+        const size_t o_cand = take(sizeof(uint4) * p.n);
+        const size_t o_flg = take(sizeof(int) * p.n);
+        const size_t o_cnt = take(sizeof(int) * 4);
+        const size_t o_st = take(sizeof(long long) * 2);
+        KMC_TRY(mws.alloc(off, s));
+        char *b = mws.as<char>();
+        ximg = reinterpret_cast<uint8_t *>(b + o_x);
+        cimg = reinterpret_cast<uint8_t *>(b + o_c);
+        nx = reinterpret_cast<float *>(b + o_nx);
+        n1 = reinterpret_cast<float *>(b + o_n1);
+        sums_km = reinterpret_cast<float *>(b + o_skm);
+        sizes32 = reinterpret_cast<float *>(b + o_s32);
+        cn2 = reinterpret_cast<float *>(b + o_cn2);
+        cn1 = reinterpret_cast<float *>(b + o_cn1);
+        consts = reinterpret_cast<MixedConsts *>(b + o_cst);
+        cand = reinterpret_cast<uint4 *>(b + o_cand);
+        flagged = reinterpret_cast<int *>(b + o_flg);
+        n_flagged = reinterpret_cast<int *>(b + o_cnt);
+        err_dev = n_flagged + 1;
+        stats = reinterpret_cast<long long *>(b + o_st);
+        KMC_CUDA_TRY(cudaMemsetAsync(consts, 0, sizeof(MixedConsts), s));
+        KMC_CUDA_TRY(cudaMemsetAsync(n_flagged, 0, sizeof(int) * 4, s));
+        KMC_CUDA_TRY(cudaMemsetAsync(stats, 0, sizeof(long long) * 2, s));
+        // one-time conversion of X (charged to the fit, reported separately)
+        absmax_kernel<<<grid1d(p.n * p.d, 256, 4096), 256, 0, s>>>(p.X, p.n * p.d,
+                                                                    &consts->xmax_bits);
+        KMC_TRY(check_launch("absmax"));
+        sigma_kernel<<<1, 1, 0, s>>>(consts, bf16);
+        KMC_TRY(check_launch("sigma"));
+        const int64_t rows = ntiles * kTileM;
+        if (bf16)
+            x_image_kernel<1><<<grid1d(rows, 256, 1 << 20), 256, 0, s>>>(p.X, p.n, p.d, nkb, rows,
+                                                                        consts, ximg, nx, n1);
+        else
+            x_image_kernel<0><<<grid1d(rows, 256, 1 << 20), 256, 0, s>>>(p.X, p.n, p.d, nkb, rows,
+                                                                        consts, ximg, nx, n1);
+        KMC_TRY(check_launch("x_image"));
+        this->launches += 3;
+        return KMC_OK;
+    }
+
+    int centroid_prep(const float *cur, const LoopState *guard) {
+        const FitParams<float, I> &p = this->prm;
+        cudaStream_t s = p.stream;
+        if (bf16)
+            c_image_kernel<1><<<grid1d(k_pad, 128, 4096), 128, 0, s>>>(cur, p.d, p.k, k_pad, nkb,
+                                                                      consts, cimg, cn2, cn1, guard);
+        else
+            c_image_kernel<0><<<grid1d(k_pad, 128, 4096), 128, 0, s>>>(cur, p.d, p.k, k_pad, nkb,
+                                                                      consts, cimg, cn2, cn1, guard);
+        KMC_TRY(check_launch("c_image"));
+        bound_kernel<<<1, 1024, 0, s>>>(cn2, cn1, this->hn, p.d, p.k, bf16, consts, guard);
+        return check_launch("bound");
+    }
+
+    int assign_pass(const float *cur, int update, const LoopState *guard) {
+        const FitParams<float, I> &p = this->prm;
+        cudaStream_t s = p.stream;
+        KMC_TRY(centroid_prep(cur, guard));
+        reset_kernel<<<grid1d(k_pad * d4 + k_pad, 256, 2048), 256, 0, s>>>(
+            sums_km, k_pad * d4, sizes32, k_pad, n_flagged, guard);
+        KMC_TRY(check_launch("mixed_reset"));
+        MixedArgs a;
+        a.ximg = ximg;
+        a.cimg = cimg;
+        a.hn = this->hn;
+        a.nx = nx;
+        a.n1 = n1;
+        a.consts = consts;
+        a.X = p.X;
+        a.w = p.w;
+        a.labels = p.labels;
+        a.sums_km = sums_km;
+        a.sizes = sizes32;
+        a.cand = cand;
+        a.flagged = flagged;
+        a.n_flagged = n_flagged;
+        a.err_global = err_dev;
+        a.guard = guard;
+        a.n = p.n;
+        a.d = p.d;
+        a.k = p.k;
+        a.k_pad = k_pad;
+        a.d4 = d4;
+        a.update = update;
+        a.label64 = sizeof(I) == 8 ? 1 : 0;
+        const SmemLayout L = smem_layout(nkb, k_pad);
+        auto kern = bf16 ? (nkb == 1 ? mixed_assign_kernel<1, 1> : mixed_assign_kernel<1, 2>)
+                         : (nkb == 1 ? mixed_assign_kernel<0, 1> : mixed_assign_kernel<0, 2>);
+        KMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)L.total));
+        const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(ntiles, num_sms()));
+        if (p.n > 0) {
+            kern<<<(unsigned)grid, kThreadsMixed, L.total, s>>>(a);
+            KMC_TRY(check_launch("mixed_assign"));
+        }
+        const int rblock = 256;
+        const size_t rsmem = sizeof(float) * (rblock / 32) * std::max<int64_t>(p.d, 1);
+        recheck_kernel<<<(unsigned)(num_sms() * 4), rblock, rsmem, s>>>(
+            p.X, p.w, cur, this->hn, cand, flagged, n_flagged, p.n, p.d, p.k, d4, p.labels,
+            a.label64, sums_km, sizes32, update, guard);
+        KMC_TRY(check_launch("mixed_recheck"));
+        stats_kernel<<<1, 1, 0, s>>>(n_flagged, stats, stats + 1, guard);
+        return check_launch("mixed_stats");
+    }
+
+    int step_assign_and_accumulate(const float *cur, int64_t *n_launches) override {
+        *n_launches = 6;
+        return assign_pass(cur, 1, this->state);
+    }
+
+    int reduce_step(float *nxt) override {
+        const FitParams<float, I> &p = this->prm;
+        cudaStream_t s = p.stream;
+        km_to_dk_kernel<<<grid1d(p.d * p.k + p.k, 256, 4096), 256, 0, s>>>(
+            sums_km, sizes32, nxt, this->sizes, p.d, p.k, d4, this->state);
+        KMC_TRY(check_launch("km_to_dk"));
+        return launch_empty_list<float, I>(this->sizes, this->empty_list, this->n_empty, p.k, s,
+                                           this->state);
+    }
+
+    int final_assignment() override { return assign_pass(this->prm.centroids, 0, nullptr); }
+
+    int counters(int64_t *last, int64_t *total, int *device_error) override {
+        long long h[2] = {0, 0};
+        int e = 0;
+        KMC_CUDA_TRY(cudaMemcpyAsync(h, stats, sizeof(h), cudaMemcpyDeviceToHost,
+                                     this->prm.stream));
+        KMC_CUDA_TRY(cudaMemcpyAsync(&e, err_dev, sizeof(int), cudaMemcpyDeviceToHost,
+                                     this->prm.stream));
+        KMC_CUDA_TRY(cudaStreamSynchronize(this->prm.stream));
+        if (last) *last = h[0];
+        if (total) *total = h[1];
+        if (device_error) *device_error = e;
+        return KMC_OK;
+    }
+};
+
 template <typename T, typename I>
-int make_mixed_fit(const FitParams<T, I> &, int, std::unique_ptr<FitBase> *) {
-    set_error("the mixed tensor-core form is not available in this build");
-    return KMC_ERR_UNSUPPORTED;
+int make_mixed_fit(const FitParams<T, I> &p, int form, std::unique_ptr<FitBase> *out) {
+    if constexpr (!std::is_same<T, float>::value) {
+        set_error("the mixed tensor-core form needs float32 data");
+        return KMC_ERR_UNSUPPORTED;
+    } else {
+        if (!MixedFit<I>::supported(p.d, p.k)) {
+            set_error("mixed form supports n_features <= 128 and n_clusters <= %d within %zu "
+                      "bytes of shared memory (got d=%lld, k=%lld)",
+                      kMaxKPad, kSmemLimit, (long long)p.d, (long long)p.k);
+            return KMC_ERR_UNSUPPORTED;
+        }
+        auto f = std::make_unique<MixedFit<I>>();
+        KMC_TRY(f->init(p));
+        KMC_TRY(f->init_mixed(form));
+        *out = std::move(f);
+        return KMC_OK;
+    }
 }
 
 template int make_mixed_fit<float, int32_t>(const FitParams<float, int32_t> &, int,

@@ -267,6 +267,14 @@ int launch_reduce_centroids(const A *sizes_cp, const A *cent_cp, T *out_sizes, T
     return check_launch("empty_clusters_list");
 }
 
+template <typename T, typename I>
+int launch_empty_list(const T *sizes, I *list, I *n_empty, int64_t k, cudaStream_t s,
+                      const LoopState *guard) {
+    if (k == 0) return KMC_OK;
+    empty_list_kernel<T, I><<<1, 1024, 0, s>>>(sizes, list, n_empty, k, guard);
+    return check_launch("empty_clusters_list");
+}
+
 template <typename T>
 int launch_shifts(const T *old_c, const T *new_c, T *out, int64_t d, int64_t k,
                   cudaStream_t s) {
@@ -334,6 +342,8 @@ int launch_fill(T *p, T v, int64_t count, cudaStream_t s, const LoopState *guard
     template int launch_reduce_centroids<T, I, T>(const T *, const T *, T *, T *, I *, I *,   \
                                                   int64_t, int64_t, int64_t, cudaStream_t,    \
                                                   const LoopState *);                         \
+    template int launch_empty_list<T, I>(const T *, I *, I *, int64_t, cudaStream_t,          \
+                                         const LoopState *);                                  \
     template int launch_inertia<T, I>(const T *, const T *, const T *, const I *, T *,        \
                                       int64_t, int64_t, int64_t, cudaStream_t,                \
                                       const LoopState *, const int64_t *);

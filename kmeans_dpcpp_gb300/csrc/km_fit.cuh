@@ -56,6 +56,13 @@ struct FitBase {
     virtual int enqueue_iteration() = 0;
     virtual int read_state(LoopState &out) = 0;
     virtual int finalize(int64_t *n_iter_out, double *inertia_out) = 0;
+    // Samples re-evaluated in exact arithmetic (mixed form): last pass and total.
+    virtual int counters(int64_t *last, int64_t *total, int *device_error) {
+        if (last) *last = 0;
+        if (total) *total = 0;
+        if (device_error) *device_error = 0;
+        return KMC_OK;
+    }
 };
 
 template <typename T, typename I>
@@ -84,6 +91,9 @@ struct PlainFit : FitBase {
     virtual int step_assign_and_accumulate(const T *cur, int64_t *n_launches);
     // Labels against the final centroids (kmeans_lloyd_driver.hpp:372-386).
     virtual int final_assignment();
+    // Private copies -> new centroid sums, sizes and the empty-cluster list
+    // (kmeans_lloyd_driver.hpp:155-170).
+    virtual int reduce_step(T *nxt);
 };
 
 // Mixed tensor-core form (kernels_mixed.cu); float32 data only.

@@ -33,6 +33,10 @@ template <typename T, typename I, typename A>
 int launch_reduce_centroids(const A *sizes_cp, const A *cent_cp, T *out_sizes, T *out_cent,
                             I *empty_list, I *n_empty, int64_t P, int64_t d, int64_t k,
                             cudaStream_t s, const LoopState *guard = nullptr);
+// Empty-cluster list in ascending order, appended from *n_empty.
+template <typename T, typename I>
+int launch_empty_list(const T *sizes, I *list, I *n_empty, int64_t k, cudaStream_t s,
+                      const LoopState *guard = nullptr);
 template <typename T>
 int launch_shifts(const T *old_c, const T *new_c, T *out, int64_t d, int64_t k,
                   cudaStream_t s);

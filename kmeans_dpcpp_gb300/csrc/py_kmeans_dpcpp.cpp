@@ -601,12 +601,47 @@ size_t py_compute_number_of_private_copies(py::object a0, size_t n, size_t d, si
 
 void print_cb(const char *line, void *) { py::print(std::string(line) + "\n"); }
 
+int form_code(const std::string &form) {
+    if (form == "plain") return KMC_FORM_PLAIN;
+    if (form == "mixed-bf16") return KMC_FORM_MIXED_BF16;
+    if (form == "mixed-fp16") return KMC_FORM_MIXED_FP16;
+    throw py::value_error("form must be 'plain', 'mixed-fp16' or 'mixed-bf16'");
+}
+
+// Mixed tensor-core forms through a fit session (same loop, same results
+// contract: init_centroid_t is overwritten, res_centroids_t holds the result).
+template <typename I>
+int64_t run_mixed_fit(const Arr &X, const Arr &w, const Arr &ic, const Arr &lab, const Arr &rc,
+                      int64_t n, int64_t d, int64_t k, double tol, int64_t max_iter, int form,
+                      const Queue &q, float *inertia_out) {
+    kmc_fit_t fit = nullptr;
+    int rc_;
+    if (sizeof(I) == 4)
+        rc_ = kmc_fit_create_f32_i32(X.data<float>(), w.data<float>(), ic.data<float>(),
+                                     lab.data<int32_t>(), rc.data<float>(), n, d, k, tol, max_iter,
+                                     form, q.stream, &fit);
+    else
+        rc_ = kmc_fit_create_f32_i64(X.data<float>(), w.data<float>(), ic.data<float>(),
+                                     lab.data<int64_t>(), rc.data<float>(), n, d, k, tol, max_iter,
+                                     form, q.stream, &fit);
+    check(rc_);
+    int64_t it = 0;
+    double inr = 0.0;
+    int r1 = kmc_fit_run(fit);
+    int r2 = (r1 == KMC_OK) ? kmc_fit_finalize(fit, &it, &inr) : r1;
+    kmc_fit_destroy(fit);
+    check(r2);
+    *inertia_out = (float)inr;
+    return it;
+}
+
 // _kmeans_lloyd.cpp:1149-1275
 std::pair<size_t, py::array> py_kmeans_lloyd_driver(py::object a0, py::object a1, py::object a2,
                                                     py::object a3, py::object a4, double tol,
                                                     bool verbose, size_t max_iter, size_t h,
                                                     size_t wgs, double occ, py::object qo,
-                                                    std::vector<Event> depends) {
+                                                    std::vector<Event> depends,
+                                                    std::string form) {
     Arr X = as_arr(a0), w = as_arr(a1), ic = as_arr(a2), lab = as_arr(a3), rc = as_arr(a4);
     Queue q = as_queue(qo);
     if (!is_2d(X) || !is_1d(w) || !is_2d(ic) || !is_2d(rc) || !is_1d(lab))
@@ -626,9 +661,24 @@ std::pair<size_t, py::array> py_kmeans_lloyd_driver(py::object a0, py::object a1
     if (occ <= 0.0 || occ >= 1.0)
         throw py::value_error("Fraction `centroids_private_copies_max_cache_occupancy` is out of bounds");
     if (tol < 0.0) throw py::value_error("Tolerance must be non-negative");
+    const int fcode = form_code(form);
     wait_on(q, depends);
     int64_t n_iters = 0;
     py::array res;
+    if (fcode != KMC_FORM_PLAIN) {
+        if (dT != DT::F32 || (iT != DT::I32 && iT != DT::I64))
+            throw py::value_error("mixed forms need float32 data and int32/int64 labels");
+        if (verbose) throw py::value_error("verbose output is only available for form='plain'");
+        auto tmp = py::array_t<float>(1);
+        float *out = tmp.mutable_data(0);
+        res = py::cast<py::array>(tmp);
+        n_iters = (iT == DT::I32)
+                      ? run_mixed_fit<int32_t>(X, w, ic, lab, rc, n, d, k, tol, (int64_t)max_iter,
+                                               fcode, q, out)
+                      : run_mixed_fit<int64_t>(X, w, ic, lab, rc, n, d, k, tol, (int64_t)max_iter,
+                                               fcode, q, out);
+        return {(size_t)n_iters, res};
+    }
 #define DRV(SUF, T, I)                                                                        \
     {                                                                                         \
         auto tmp = py::array_t<T>(1);                                                         \
@@ -741,5 +791,6 @@ PYBIND11_MODULE(_kmeans_dpcpp, m) {
           py::arg("assignments_id"), py::arg("res_centroids_t"), py::arg("tol"),
           py::arg("verbose"), py::arg("max_iter"), py::arg("centroids_window_height"),
           py::arg("work_group_size"), py::arg("centroids_private_copies_max_cache_occupancy"),
-          py::arg("sycl_queue"), py::arg("depends") = std::vector<Event>());
+          py::arg("sycl_queue"), py::arg("depends") = std::vector<Event>(),
+          py::arg("form") = std::string("plain"));
 }

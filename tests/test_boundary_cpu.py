@@ -53,6 +53,8 @@ REFERENCE_SIGNATURES = {
                             "centroids_private_copies_max_cache_occupancy", "sycl_queue",
                             "depends"],
 }
+# Trailing keyword arguments this engine adds after the reference's list.
+EXTRA_KWARGS = {"kmeans_lloyd_driver": ["form"]}
 
 
 def test_library_exports_every_declared_symbol():
@@ -72,7 +74,7 @@ def test_module_surface_matches_reference():
         fn = getattr(kdp, name)
         sig = fn.__doc__.splitlines()[0]
         got = re.findall(r"(\w+): ", sig[sig.index("(") + 1:])
-        assert got == args, (name, got)
+        assert got == args + EXTRA_KWARGS.get(name, []), (name, got)
 
 
 def _py_private_copies(esize, n, d, k, occ, wgs, l2):
@@ -192,6 +194,15 @@ def test_python_surface_validation_messages(call, msg):
     with pytest.raises(ValueError) as ei:
         call(kdp, FakeStream())
     assert str(ei.value) == msg
+
+
+def test_driver_rejects_unknown_form():
+    import kmeans_dpcpp_gb300 as kdp
+
+    with pytest.raises(ValueError) as ei:
+        kdp.kmeans_lloyd_driver(F(3, 10), F(10), F(3, 4), I4(10), F(3, 4), 1e-4, False, 10, 8, 32,
+                                0.5, FakeStream(), form="int8")
+    assert "form must be" in str(ei.value)
 
 
 def test_compute_threshold_topk_zero_is_noop():

@@ -1,0 +1,113 @@
+"""Mixed tensor-core forms (fp16 / bf16 operands, fp32 accumulation) vs the oracle.
+
+Labels from one mixed assignment pass must equal the exact reference labels
+for every sample: samples whose tensor-core margin does not certify them are
+re-evaluated in exact float32.  Full fits accumulate centroid sums in float32
+atomics, so their trajectories are compared with tolerances: labels identical
+except for samples whose top-two relative gap is below 1e-5, centroids and
+inertia within 1e-5 relative.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import bench
+
+pytestmark = pytest.mark.gpu
+
+FORMS = {"fp16": 2, "bf16": 1}
+
+
+def _fit_labels(X, C0, form, max_iter=0, tol=0.0):
+    import torch
+
+    from kmeans_dpcpp_gb300 import capi
+
+    L = capi.lib()
+    d, n = X.shape
+    k = C0.shape[1]
+    Xg = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+    w = torch.ones(n, dtype=torch.float32, device="cuda")
+    cur = torch.from_numpy(np.ascontiguousarray(C0).copy()).cuda()
+    res = torch.empty_like(cur)
+    lab = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    fit = ctypes.c_void_p()
+    capi.check(L.kmc_fit_create_f32_i32(Xg.data_ptr(), w.data_ptr(), cur.data_ptr(), lab.data_ptr(),
+                                        res.data_ptr(), n, d, k, tol, max_iter, form,
+                                        stream.cuda_stream, ctypes.byref(fit)))
+    try:
+        capi.check(L.kmc_fit_run(fit))
+        it, inertia = ctypes.c_int64(), ctypes.c_double()
+        capi.check(L.kmc_fit_finalize(fit, ctypes.byref(it), ctypes.byref(inertia)))
+        last, total, err = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
+        capi.check(L.kmc_fit_rechecked(fit, ctypes.byref(last), ctypes.byref(total), ctypes.byref(err)))
+    finally:
+        capi.check(L.kmc_fit_destroy(fit))
+    assert err.value == 0, "tensor-core kernel reported a device-side timeout"
+    return it.value, lab.cpu().numpy(), res.cpu().numpy(), inertia.value, last.value, total.value
+
+
+SHAPES = [(300, 64, 256), (1000, 3, 8), (5000, 14, 127), (20000, 64, 1024), (7777, 100, 300),
+          (4096, 33, 511), (129, 128, 512), (20000, 16, 1024), (3001, 65, 257)]
+
+
+@pytest.mark.parametrize("n,d,k", SHAPES)
+@pytest.mark.parametrize("form", sorted(FORMS))
+def test_mixed_assignment_equals_reference_labels(oracle, n, d, k, form):
+    X, _, _ = bench.make_blobs(n, d, max(1, k // 2), (-5, 5), 1.0, seed=n + d + k)
+    if k <= n:
+        C0 = bench.random_row_init(X, k, seed=k)
+    else:
+        C0 = np.random.default_rng(k).uniform(-5, 5, (d, k)).astype(np.float32)
+    _, lab, _, _, last, _ = _fit_labels(X, C0, FORMS[form])
+    np.testing.assert_array_equal(lab, oracle.assignment(X, C0))
+    assert 0 <= last <= n
+
+
+@pytest.mark.parametrize("d,k", [(64, 1025), (129, 64), (100, 513)])
+def test_mixed_rejects_unsupported_shapes(d, k):
+    X = np.zeros((d, 256), np.float32)
+    C = np.zeros((d, k), np.float32)
+    with pytest.raises(RuntimeError, match="kmc error 4"):
+        _fit_labels(X, C, FORMS["fp16"])
+
+
+@pytest.mark.parametrize("form", sorted(FORMS))
+def test_mixed_assignment_ties_and_duplicates(oracle, form):
+    rng = np.random.default_rng(5)
+    C = rng.standard_normal((64, 128)).astype(np.float32)
+    C = np.ascontiguousarray(np.concatenate([C, C], axis=1))   # exact duplicates: all ties
+    X = rng.standard_normal((64, 3000)).astype(np.float32)
+    _, lab, _, _, last, _ = _fit_labels(X, C, FORMS[form])
+    np.testing.assert_array_equal(lab, oracle.assignment(X, C))
+    assert last == 3000          # every sample ties between j and j + 128
+    assert lab.max() < 128
+
+
+def _near_tie_mask(X, C, rel=1e-5):
+    """Samples whose two smallest distances differ by less than rel (relative)."""
+    d2 = np.maximum(0.0, (X.astype(np.float64) ** 2).sum(0)[:, None]
+                    - 2 * X.T.astype(np.float64) @ C.astype(np.float64)
+                    + (C.astype(np.float64) ** 2).sum(0)[None, :])
+    part = np.partition(d2, 1, axis=1)[:, :2]
+    return (part[:, 1] - part[:, 0]) <= rel * np.maximum(part[:, 1], 1e-30)
+
+
+@pytest.mark.parametrize("case", [("c1_50k_d14_k16", 50_000, 14, 16, 16, (-10, 10), 1.0, 0, 1e-4, 100),
+                                  ("d64_k256", 60_000, 64, 256, 256, (-5, 5), 1.0, 2, 0.0, 8),
+                                  ("d64_k1024_sigma", 100_000, 64, 1024, 1024, (-5, 5), (0.5, 2.0), 2,
+                                   0.0, 5)])
+@pytest.mark.parametrize("form", sorted(FORMS))
+def test_mixed_driver_tracks_oracle(oracle, case, form):
+    name, n, d, centers, k, box, std, seed, tol, max_iter = case
+    X, _, _ = bench.make_blobs(n, d, centers, box, std, seed)
+    C0 = bench.random_row_init(X, k, seed)
+    it_o, lab_o, C_o, inr_o, _ = oracle.kmeans_lloyd_driver(X, np.ones(n, np.float32), C0, tol, max_iter)
+    it_g, lab_g, C_g, inr_g, _, total = _fit_labels(X, C0, FORMS[form], max_iter=max_iter, tol=tol)
+    assert it_g == it_o
+    diff = lab_g != lab_o
+    assert not np.any(diff & ~_near_tie_mask(X, C_o)), int(diff.sum())
+    np.testing.assert_allclose(C_g, C_o, rtol=1e-5, atol=1e-5 * np.abs(C_o).max())
+    assert inr_g == pytest.approx(inr_o, rel=1e-5)
