@@ -87,8 +87,10 @@ struct MixedArgs {
     const float *X;
     const float *w;
     void *labels;
-    float *sums_km;
-    float *sizes;
+    float *sums32;     // [k_pad][d4] fp32 cluster sums (vector-red path)
+    float *sizes32;    // [k_pad]
+    double *acc64;     // [k_pad*d4 + k_pad] fp64 sums then sizes (shared-memory path)
+    float *xflag;      // [n][d4] rows of samples sent to the exact recheck
     uint4 *cand;
     int *flagged;
     int *n_flagged;
@@ -97,13 +99,18 @@ struct MixedArgs {
     int64_t n, d, k, k_pad, d4;
     int update;
     int label64;
+    int priv64;        // accumulate in fp64 in shared memory, flushed once per CTA
+    int keep_p1;       // exact sub-chunk hot masks from shared memory
 };
 
 struct SmemLayout {
-    size_t c, x, hn, xch, lab, bar, total;
+    size_t c, x, hn, xch, lab, bar, priv, p1, total;
 };
 
-__host__ __device__ inline SmemLayout smem_layout(int nkb, int64_t k_pad) {
+// p1: sub-chunk maxima of every epilogue thread (k_pad / 64 floats each), kept
+// so that uncertified samples get exact candidate masks.
+__host__ __device__ inline SmemLayout smem_layout(int nkb, int64_t k_pad, int64_t d4 = 0,
+                                                  int priv64 = 0, int keep_p1 = 0) {
     SmemLayout L;
     size_t off = 0;
     L.c = off;
@@ -120,6 +127,11 @@ __host__ __device__ inline SmemLayout smem_layout(int nkb, int64_t k_pad) {
     off = (off + 15) & ~size_t(15);
     L.bar = off;
     off += 8 * 18 + 16;
+    off = (off + 15) & ~size_t(15);
+    L.priv = off;
+    if (priv64) off += sizeof(double) * (size_t)(k_pad * d4 + k_pad);
+    L.p1 = off;
+    if (keep_p1) off += sizeof(float) * 32 * kEpiWarps * (size_t)(k_pad / 64);
     L.total = off + 1024;  // slack for aligning the dynamic shared memory base
     return L;
 }
@@ -146,6 +158,12 @@ __device__ __forceinline__ bool epi_any(bool v) {
 
 __device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
+// Position of the n-th (0-based) set bit of m (m has more than n set bits).
+__device__ __forceinline__ int nth_set_bit(uint32_t m, int n) {
+    for (int q = 0; q < n; ++q) m &= m - 1u;
+    return __ffs(m) - 1;
+}
+
 template <int BF16, int NKB>
 __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArgs a) {
     constexpr int kStages = stages_for(NKB);
@@ -156,8 +174,10 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
     uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     const int64_t k_pad = a.k_pad;
     const int nch = (int)(k_pad / kChunkN);
-    const SmemLayout L = smem_layout(NKB, k_pad);
+    const SmemLayout L = smem_layout(NKB, k_pad, a.d4, a.priv64, a.keep_p1);
     uint8_t *cimg_s = smem + L.c;
+    double *priv = reinterpret_cast<double *>(smem + L.priv);
+    float *p1s = reinterpret_cast<float *>(smem + L.p1);
     uint8_t *xring = smem + L.x;
     float *hn_s = reinterpret_cast<float *>(smem + L.hn);
     float *xch = reinterpret_cast<float *>(smem + L.xch);
@@ -191,6 +211,8 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
     }
     for (int64_t j = threadIdx.x; j < k_pad; j += blockDim.x)
         hn_s[j] = (j < k) ? a.hn[j] : pos_inf<float>();
+    if (a.priv64)
+        for (int64_t e = threadIdx.x; e < k_pad * a.d4 + k_pad; e += blockDim.x) priv[e] = 0.0;
     if (warp == 1) {
         tmem_alloc(tmem_slot, 512);
         tmem_relinquish();
@@ -281,12 +303,30 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
         const uint32_t lane_addr = (uint32_t)(32 * q) << 16;
         uint32_t cnt = 0;
         int tl = 0;
+        const int nsc_h = (int)(k_pad / 64);  // sub-chunks per column half
+        float *my_p1 = p1s + (size_t)(ew * 32 + lane) * nsc_h;
+        // per-sample norms of the next tile are loaded one tile ahead
+        float nx_next = 0.f, n1_next = 0.f;
+        {
+            const int64_t i0 = (int64_t)blockIdx.x * kTileM + row;
+            if (i0 < n) {
+                nx_next = a.nx[i0];
+                n1_next = a.n1[i0];
+            }
+        }
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tl) {
             const int64_t i = tile * kTileM + row;
             float E2 = 0.f;
             if (i < n) {
-                float e = fmaf(a.nx[i], cst.alpha, fmaf(a.n1[i], cst.beta1, cst.beta0));
+                float e = fmaf(nx_next, cst.alpha, fmaf(n1_next, cst.beta1, cst.beta0));
                 E2 = 2.f * e * 1.000001f;
+            }
+            {
+                const int64_t inext = (tile + gridDim.x) * kTileM + row;
+                if (inext < n) {
+                    nx_next = a.nx[inext];
+                    n1_next = a.n1[inext];
+                }
             }
             float P2[32];
 #pragma unroll
@@ -304,11 +344,9 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                     break;
                 }
                 tc_fence_after();
-#pragma unroll 1
-                for (int qq = 0; qq < 4; ++qq) {
-                    uint32_t r[32];
-                    tmem_ld32(tmem + lane_addr + b * kChunkN + h * 128 + qq * 32, r);
-                    tmem_ld_wait();
+                const uint32_t cbase = tmem + lane_addr + b * kChunkN + h * 128;
+                // one 32-column sub-chunk: scores, class maxima, sub-chunk maximum
+                auto process = [&](const uint32_t (&r)[32], int qq) {
                     const int j0 = c * kChunkN + h * 128 + qq * 32;
                     const float4 *hv = reinterpret_cast<const float4 *>(hn_s + j0);
                     float v[32];
@@ -322,7 +360,6 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                     }
 #pragma unroll
                     for (int t = 0; t < 32; ++t) P2[t] = fmaxf(P2[t], v[t]);
-                    // sub-chunk maximum: ternary tree
                     float m11[11];
 #pragma unroll
                     for (int u = 0; u < 10; ++u) m11[u] = max3f(v[3 * u], v[3 * u + 1], v[3 * u + 2]);
@@ -340,15 +377,33 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                     } else if (m > R1) {
                         R1 = m;
                     }
-                    // superset of the final hot sub-chunks: the final threshold
-                    // M - 2E is at least Mrun - 2E
-                    if (m >= Mrun - E2) hot1 |= 1u << sidx;
-                }
+                    if (a.keep_p1) {
+                        my_p1[sidx] = m;
+                    } else {
+                        // superset of the final hot sub-chunks: the final
+                        // threshold M - 2E is at least Mrun - 2E
+                        if (m >= Mrun - E2) hot1 |= 1u << sidx;
+                    }
+                };
+                // double-buffered TMEM loads: the next sub-chunk is in flight
+                // while the current one is processed
+                uint32_t ra[32], rb[32];
+                tmem_ld32(cbase + 0, ra);
+                tmem_ld_wait();
+                tmem_ld32(cbase + 32, rb);
+                process(ra, 0);
+                tmem_ld_wait();
+                tmem_ld32(cbase + 64, ra);
+                process(rb, 1);
+                tmem_ld_wait();
+                tmem_ld32(cbase + 96, rb);
+                process(ra, 2);
+                tmem_ld_wait();
                 tc_fence_before();
-                mbar_arrive(&tempty[b]);
+                mbar_arrive(&tempty[b]);  // the accumulator may be overwritten now
+                process(rb, 3);
                 ++cnt;
             }
-            if (epi_any(bad || *err != 0)) break;
 
             // winner and runner-up within this column half
             float M2 = -pos_inf<float>(), R2 = -pos_inf<float>();
@@ -370,7 +425,8 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
             xb[(h * kTileM + row) * 3 + 0] = Mh;
             xb[(h * kTileM + row) * 3 + 1] = __int_as_float(jh);
             xb[(h * kTileM + row) * 3 + 2] = Rh;
-            epi_sync();
+            // one barrier per tile: publishes the exchange and agrees on errors
+            if (epi_any(bad || *err != 0)) break;
             const float Mo = xb[((h ^ 1) * kTileM + row) * 3 + 0];
             const int jo = __float_as_int(xb[((h ^ 1) * kTileM + row) * 3 + 1]);
             const float Ro = xb[((h ^ 1) * kTileM + row) * 3 + 2];
@@ -390,6 +446,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                 R = Mh;  // tie (or both -inf): not certified
             }
             const bool cert = (M - R) > E2;  // false for NaN / infinities
+            int code = -1;  // handoff to the update warps: >= 0 label, <= -2 recheck slot
             if (i < n) {
                 if (!cert) {
                     const float thr = M - E2;
@@ -397,54 +454,107 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
 #pragma unroll
                     for (int t = 0; t < 32; ++t)
                         if (P2[t] >= thr) hot2 |= 1u << t;
+                    if (a.keep_p1) {
+                        hot1 = 0u;
+                        for (int sc = 0; sc < nsc_h; ++sc)
+                            if (my_p1[sc] >= thr) hot1 |= 1u << sc;
+                    }
                     uint32_t *cw = reinterpret_cast<uint32_t *>(a.cand + i);
                     cw[h] = hot1;
                     cw[2 + h] = hot2;
                     if (h == 0) {
-                        int pos = atomicAdd(a.n_flagged, 1);
-                        if (pos >= 0 && pos < n) a.flagged[pos] = (int)i;
+                        const int pos = atomicAdd(a.n_flagged, 1);
+                        if (pos >= 0 && pos < n) {
+                            a.flagged[pos] = (int)i;
+                            code = -2 - pos;
+                        }
                     }
-                } else if (h == 0) {
-                    if (a.label64)
-                        reinterpret_cast<int64_t *>(a.labels)[i] = jw;
-                    else
-                        reinterpret_cast<int32_t *>(a.labels)[i] = jw;
+                } else {
+                    code = jw;
+                    if (h == 0) {
+                        if (a.label64)
+                            reinterpret_cast<int64_t *>(a.labels)[i] = jw;
+                        else
+                            reinterpret_cast<int32_t *>(a.labels)[i] = jw;
+                    }
                 }
             }
-            if (a.update && h == 0) {
+            if (h == 0) {
                 const int tb = tl & 1;
-                if (!mbar_wait(&uempty[tb], (((uint32_t)tl >> 1) & 1u) ^ 1u, err)) bad = true;
-                lab_s[tb * kTileM + row] = (cert && i < n) ? jw : -1;
-                mbar_arrive(&ufull[tb]);
+                if (mbar_wait(&uempty[tb], (((uint32_t)tl >> 1) & 1u) ^ 1u, err)) {
+                    lab_s[tb * kTileM + row] = code;
+                    mbar_arrive(&ufull[tb]);
+                }
             }
-            if (epi_any(bad)) break;
         }
     } else {
         // ------------------------------ update --------------------------------
-        if (a.update) {
-            const int row = threadIdx.x - 32 * (2 + kEpiWarps);
-            const int64_t d = a.d, d4 = a.d4;
-            int tl = 0;
-            for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tl) {
-                const int tb = tl & 1;
-                if (!mbar_wait(&ufull[tb], ((uint32_t)tl >> 1) & 1u, err)) break;
-                const int lab = lab_s[tb * kTileM + row];
-                mbar_arrive(&uempty[tb]);
-                const int64_t i = tile * kTileM + row;
-                if (lab >= 0 && lab < k && i < n) {
-                    const float wv = a.w[i];
-                    float4 *dst = reinterpret_cast<float4 *>(a.sums_km + (int64_t)lab * d4);
-                    for (int64_t g = 0; g < d4 / 4; ++g) {
-                        const int64_t f = 4 * g;
-                        float4 v;
-                        v.x = (f + 0 < d) ? __fmul_rn(a.X[(f + 0) * n + i], wv) : 0.f;
-                        v.y = (f + 1 < d) ? __fmul_rn(a.X[(f + 1) * n + i], wv) : 0.f;
-                        v.z = (f + 2 < d) ? __fmul_rn(a.X[(f + 2) * n + i], wv) : 0.f;
-                        v.w = (f + 3 < d) ? __fmul_rn(a.X[(f + 3) * n + i], wv) : 0.f;
-                        atomicAdd(dst + g, v);
-                    }
-                    atomicAdd(a.sizes + lab, wv);
+        // One thread per tile row.  The row's features are loaded before its
+        // label is known, so the loads overlap the epilogue of the same tile.
+        const int row = threadIdx.x - 32 * (2 + kEpiWarps);
+        const int64_t d = a.d, d4 = a.d4;
+        int tl = 0;
+        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tl) {
+            const int tb = tl & 1;
+            const int64_t i = tile * kTileM + row;
+            int code = -1;
+            bool have_code = false;
+            float wv = 0.f;
+#pragma unroll 1
+            for (int pass = 0; pass < NKB; ++pass) {
+                float xv[64];
+#pragma unroll
+                for (int f = 0; f < 64; ++f) {
+                    const int64_t F = (int64_t)pass * 64 + f;
+                    xv[f] = (i < n && F < d) ? __ldg(a.X + F * n + i) : 0.f;
                 }
+                if (!have_code) {
+                    if (!mbar_wait(&ufull[tb], ((uint32_t)tl >> 1) & 1u, err)) break;
+                    code = lab_s[tb * kTileM + row];
+                    mbar_arrive(&uempty[tb]);
+                    have_code = true;
+                    if (code >= 0 && a.update) wv = a.w[i];
+                }
+                if (code >= 0 && code < k && a.update) {
+                    if (a.priv64) {
+                        double *ps = priv + (int64_t)code * d4 + pass * 64;
+#pragma unroll
+                        for (int f = 0; f < 64; ++f)
+                            if ((int64_t)pass * 64 + f < d) atomicAdd(ps + f, (double)__fmul_rn(xv[f], wv));
+                        if (pass == 0) atomicAdd(priv + k_pad * d4 + code, (double)wv);
+                    } else {
+                        float4 *dst = reinterpret_cast<float4 *>(a.sums32 + (int64_t)code * d4 + pass * 64);
+#pragma unroll
+                        for (int g = 0; g < 16; ++g) {
+                            if ((int64_t)pass * 64 + 4 * g < d4) {
+                                float4 v;
+                                v.x = __fmul_rn(xv[4 * g + 0], wv);
+                                v.y = __fmul_rn(xv[4 * g + 1], wv);
+                                v.z = __fmul_rn(xv[4 * g + 2], wv);
+                                v.w = __fmul_rn(xv[4 * g + 3], wv);
+                                atomicAdd(dst + g, v);
+                            }
+                        }
+                        if (pass == 0) atomicAdd(a.sizes32 + code, wv);
+                    }
+                } else if (code <= -2) {
+                    // stage the row for the exact recheck (contiguous, fp32)
+                    const int64_t pos = -2 - (int64_t)code;
+                    float4 *dst = reinterpret_cast<float4 *>(a.xflag + pos * d4 + pass * 64);
+#pragma unroll
+                    for (int g = 0; g < 16; ++g)
+                        if ((int64_t)pass * 64 + 4 * g < d4)
+                            dst[g] = make_float4(xv[4 * g], xv[4 * g + 1], xv[4 * g + 2], xv[4 * g + 3]);
+                }
+            }
+            if (!have_code) break;
+        }
+        if (a.priv64) {
+            // all update threads are done with the shared sums: flush them
+            asm volatile("bar.sync 2, 128;" ::: "memory");
+            for (int64_t e = row; e < k_pad * d4 + k_pad; e += kTileM) {
+                const double v = priv[e];
+                if (v != 0.0) atomicAdd(a.acc64 + e, v);
             }
         }
     }
@@ -536,7 +646,7 @@ __global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int nkb, in
 template <int BF16>
 __global__ void c_image_kernel(const float *C, int64_t d, int64_t k, int64_t k_pad, int nkb,
                                const MixedConsts *c, uint8_t *img, float *cn2, float *cn1,
-                               const LoopState *guard) {
+                               float *ct, int64_t d4, const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
     const float sigma = c->sigma;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < k_pad;
@@ -553,6 +663,7 @@ __global__ void c_image_kernel(const float *C, int64_t d, int64_t k, int64_t k_p
                     s2 += (double)x * (double)x;
                     s1 += fabs((double)x);
                     v[e] = x * sigma;
+                    if (f < d4) ct[j * d4 + f] = x;
                 }
                 uint4 pk;
                 pk.x = pack2<BF16>(v[0], v[1]);
@@ -615,45 +726,61 @@ __global__ void bound_kernel(const float *cn2, const float *cn1, const float *hn
 
 // Exact fp32 re-evaluation of samples whose margin did not certify them: the
 // reference's arithmetic (sequential fma dot, hn - dot, strict < in
-// ascending centroid order) over the candidate set, one warp per sample.
-__global__ void recheck_kernel(const float *X, const float *w, const float *C, const float *hn,
-                               const uint4 *cand, const int *flagged, const int *n_flagged,
-                               int64_t n, int64_t d, int64_t k, int64_t d4, void *labels,
-                               int label64, float *sums_km, float *sizes, int update,
+// ascending centroid order) over the candidate set, one warp per sample.  The
+// sample's features come from the compact rows staged by the update warps and
+// the centroids from their transposed fp32 copy (one contiguous row each).
+__global__ void recheck_kernel(const float *xflag, const float *ct, const float *hn,
+                               const float *w, const uint4 *cand, const int *flagged,
+                               const int *n_flagged, int64_t n, int64_t d, int64_t k, int64_t d4,
+                               void *labels, int label64, int update, int priv64, float *sums32,
+                               float *sizes32, double *acc64, int64_t k_pad,
                                const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
-    extern __shared__ float xs[];  // [warps][d]
+    extern __shared__ __align__(16) float xs[];  // [warps][d4]
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    float *x = xs + (size_t)wib * d;
+    float *x = xs + (size_t)wib * d4;
     const int64_t nf = (int64_t)*n_flagged;
     const int64_t total = nf < n ? nf : n;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t e = blockIdx.x * (int64_t)(blockDim.x >> 5) + wib; e < total; e += nwarps) {
         const int64_t i = flagged[e];
         if (i < 0 || i >= n) continue;
-        for (int64_t f = lane; f < d; f += 32) x[f] = X[f * n + i];
+        for (int64_t f = lane; f < d4; f += 32) x[f] = xflag[e * d4 + f];
         __syncwarp();
         const uint4 cm = cand[i];
         const uint32_t h1[2] = {cm.x, cm.y}, h2[2] = {cm.z, cm.w};
+        // candidate columns (sub-chunk x class) of both halves; lane L takes
+        // candidates L, L + 32, ...
+        const int n2[2] = {__popc(h2[0]), __popc(h2[1])};
+        const int ncand = __popc(h1[0]) * n2[0] + __popc(h1[1]) * n2[1];
         float best = pos_inf<float>();
         int bj = 0;
-        int idx = 0;
-        for (int h = 0; h < 2; ++h) {
-            for (uint32_t m1 = h1[h]; m1 != 0u; m1 &= m1 - 1u) {
-                const int s = __ffs(m1) - 1;
-                for (uint32_t m2 = h2[h]; m2 != 0u; m2 &= m2 - 1u, ++idx) {
-                    if ((idx & 31) != lane) continue;
-                    const int t = __ffs(m2) - 1;
-                    const int64_t j = (int64_t)(s >> 2) * kChunkN + h * 128 + (s & 3) * 32 + t;
-                    if (j >= k) continue;
-                    float dot = 0.f;
-                    for (int64_t f = 0; f < d; ++f) dot = __fmaf_rn(x[f], C[f * k + j], dot);
-                    const float D = hn[j] - dot;
-                    if (D < best || (D == best && j < bj)) {
-                        best = D;
-                        bj = (int)j;
-                    }
-                }
+        for (int q = lane; q < ncand; q += 32) {
+            int r = q, h = 0;
+            if (r >= __popc(h1[0]) * n2[0]) {
+                r -= __popc(h1[0]) * n2[0];
+                h = 1;
+            }
+            const int si = r / n2[h], ti = r % n2[h];
+            const int s = nth_set_bit(h1[h], si);
+            const int t = nth_set_bit(h2[h], ti);
+            const int64_t j = (int64_t)(s >> 2) * kChunkN + h * 128 + (s & 3) * 32 + t;
+            if (j >= k) continue;
+            const float4 *cr = reinterpret_cast<const float4 *>(ct + j * d4);
+            const float4 *xr = reinterpret_cast<const float4 *>(x);
+            float dot = 0.f;
+            for (int64_t g = 0; g < d4 / 4; ++g) {
+                const float4 cv = __ldg(cr + g);
+                const float4 xv = xr[g];
+                dot = __fmaf_rn(xv.x, cv.x, dot);
+                if (4 * g + 1 < d) dot = __fmaf_rn(xv.y, cv.y, dot);
+                if (4 * g + 2 < d) dot = __fmaf_rn(xv.z, cv.z, dot);
+                if (4 * g + 3 < d) dot = __fmaf_rn(xv.w, cv.w, dot);
+            }
+            const float D = hn[j] - dot;
+            if (D < best || (D == best && j < bj)) {
+                best = D;
+                bj = (int)j;
             }
         }
         for (int off = 16; off > 0; off >>= 1) {
@@ -672,16 +799,28 @@ __global__ void recheck_kernel(const float *X, const float *w, const float *C, c
         }
         if (update) {
             const float wv = w[i];
-            for (int64_t f = lane; f < d; f += 32)
-                atomicAdd(sums_km + (int64_t)bj * d4 + f, __fmul_rn(x[f], wv));
-            if (lane == 0) atomicAdd(sizes + bj, wv);
+            for (int64_t f = lane; f < d; f += 32) {
+                const float v = __fmul_rn(x[f], wv);
+                if (priv64)
+                    atomicAdd(acc64 + (int64_t)bj * d4 + f, (double)v);
+                else
+                    atomicAdd(sums32 + (int64_t)bj * d4 + f, v);
+            }
+            if (lane == 0) {
+                if (priv64)
+                    atomicAdd(acc64 + k_pad * d4 + bj, (double)wv);
+                else
+                    atomicAdd(sizes32 + bj, wv);
+            }
         }
         __syncwarp();
     }
 }
 
-// Cluster-major fp32 sums -> (d, k) centroid sums and sizes in dataT.
-__global__ void km_to_dk_kernel(const float *sums_km, const float *sizes32, float *out_c,
+// Cluster-major sums (fp32 or fp64) -> (d, k) centroid sums and sizes in
+// dataT, rounded once.
+template <typename A>
+__global__ void km_to_dk_kernel(const A *sums_km, const A *sizes_acc, float *out_c,
                                 float *out_sizes, int64_t d, int64_t k, int64_t d4,
                                 const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
@@ -689,22 +828,25 @@ __global__ void km_to_dk_kernel(const float *sums_km, const float *sizes32, floa
          e += (int64_t)gridDim.x * blockDim.x) {
         if (e < d * k) {
             const int64_t f = e / k, j = e % k;
-            out_c[e] = sums_km[j * d4 + f];
+            out_c[e] = (float)sums_km[j * d4 + f];
         } else {
-            out_sizes[e - d * k] = sizes32[e - d * k];
+            out_sizes[e - d * k] = (float)sizes_acc[e - d * k];
         }
     }
 }
 
-__global__ void reset_kernel(float *sums_km, int64_t count, float *sizes, int64_t k_pad,
-                             int *n_flagged, const LoopState *guard) {
+__global__ void reset_kernel(float *sums32, float *sizes32, double *acc64, int64_t count,
+                             int64_t k_pad, int priv64, int *n_flagged, const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count + k_pad;
          e += (int64_t)gridDim.x * blockDim.x) {
-        if (e < count)
-            sums_km[e] = 0.f;
-        else
-            sizes[e - count] = 0.f;
+        if (priv64) {
+            acc64[e] = 0.0;
+        } else if (e < count) {
+            sums32[e] = 0.f;
+        } else {
+            sizes32[e - count] = 0.f;
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *n_flagged = 0;
 }
@@ -730,10 +872,14 @@ struct MixedFit : PlainFit<float, I> {
     using Base = PlainFit<float, I>;
     int bf16 = 0;
     int nkb = 1;
+    int priv64 = 0;
+    int keep_p1 = 0;
     int64_t k_pad = 0, d4 = 0, ntiles = 0;
     Scratch mws;
     uint8_t *ximg = nullptr, *cimg = nullptr;
-    float *nx = nullptr, *n1 = nullptr, *sums_km = nullptr, *sizes32 = nullptr;
+    float *nx = nullptr, *n1 = nullptr, *ct = nullptr, *xflag = nullptr;
+    float *sums32 = nullptr, *sizes32 = nullptr;
+    double *acc64 = nullptr;
     float *cn2 = nullptr, *cn1 = nullptr;
     MixedConsts *consts = nullptr;
     uint4 *cand = nullptr;
@@ -755,6 +901,9 @@ struct MixedFit : PlainFit<float, I> {
         k_pad = ceil_div<int64_t>(p.k, kChunkN) * kChunkN;
         d4 = ceil_div<int64_t>(std::max<int64_t>(p.d, 1), 4) * 4;
         ntiles = ceil_div<int64_t>(p.n, kTileM);
+        // float64 sums in shared memory when they fit next to the operands
+        priv64 = smem_layout(nkb, k_pad, d4, 1).total <= kSmemLimit ? 1 : 0;
+        keep_p1 = smem_layout(nkb, k_pad, d4, priv64, 1).total <= kSmemLimit ? 1 : 0;
         size_t off = 0;
         auto take = [&](size_t bytes) {
             size_t o = off;
@@ -763,10 +912,12 @@ struct MixedFit : PlainFit<float, I> {
         };
         const size_t o_x = take((size_t)std::max<int64_t>(ntiles, 1) * nkb * kTileBytes);
         const size_t o_c = take((size_t)nkb * k_pad * 128);
+        const size_t o_ct = take(sizeof(float) * k_pad * d4);
         const size_t o_nx = take(sizeof(float) * p.n);
         const size_t o_n1 = take(sizeof(float) * p.n);
-        const size_t o_skm = take(sizeof(float) * k_pad * d4);
-        const size_t o_s32 = take(sizeof(float) * k_pad);
+        const size_t o_s32 = take(priv64 ? 16 : sizeof(float) * (k_pad * d4 + k_pad));
+        const size_t o_a64 = take(priv64 ? sizeof(double) * (k_pad * d4 + k_pad) : 16);
+        const size_t o_xf = take(sizeof(float) * std::max<int64_t>(p.n, 1) * d4);
         const size_t o_cn2 = take(sizeof(float) * p.k);
         const size_t o_cn1 = take(sizeof(float) * p.k);
         const size_t o_cst = take(sizeof(MixedConsts));
@@ -778,10 +929,13 @@ struct MixedFit : PlainFit<float, I> {
         char *b = mws.as<char>();
         ximg = reinterpret_cast<uint8_t *>(b + o_x);
         cimg = reinterpret_cast<uint8_t *>(b + o_c);
+        ct = reinterpret_cast<float *>(b + o_ct);
         nx = reinterpret_cast<float *>(b + o_nx);
         n1 = reinterpret_cast<float *>(b + o_n1);
-        sums_km = reinterpret_cast<float *>(b + o_skm);
-        sizes32 = reinterpret_cast<float *>(b + o_s32);
+        sums32 = reinterpret_cast<float *>(b + o_s32);
+        sizes32 = sums32 + k_pad * d4;
+        acc64 = reinterpret_cast<double *>(b + o_a64);
+        xflag = reinterpret_cast<float *>(b + o_xf);
         cn2 = reinterpret_cast<float *>(b + o_cn2);
         cn1 = reinterpret_cast<float *>(b + o_cn1);
         consts = reinterpret_cast<MixedConsts *>(b + o_cst);
@@ -815,11 +969,11 @@ struct MixedFit : PlainFit<float, I> {
         const FitParams<float, I> &p = this->prm;
         cudaStream_t s = p.stream;
         if (bf16)
-            c_image_kernel<1><<<grid1d(k_pad, 128, 4096), 128, 0, s>>>(cur, p.d, p.k, k_pad, nkb,
-                                                                      consts, cimg, cn2, cn1, guard);
+            c_image_kernel<1><<<grid1d(k_pad, 128, 4096), 128, 0, s>>>(
+                cur, p.d, p.k, k_pad, nkb, consts, cimg, cn2, cn1, ct, d4, guard);
         else
-            c_image_kernel<0><<<grid1d(k_pad, 128, 4096), 128, 0, s>>>(cur, p.d, p.k, k_pad, nkb,
-                                                                      consts, cimg, cn2, cn1, guard);
+            c_image_kernel<0><<<grid1d(k_pad, 128, 4096), 128, 0, s>>>(
+                cur, p.d, p.k, k_pad, nkb, consts, cimg, cn2, cn1, ct, d4, guard);
         KMC_TRY(check_launch("c_image"));
         bound_kernel<<<1, 1024, 0, s>>>(cn2, cn1, this->hn, p.d, p.k, bf16, consts, guard);
         return check_launch("bound");
@@ -830,7 +984,7 @@ struct MixedFit : PlainFit<float, I> {
         cudaStream_t s = p.stream;
         KMC_TRY(centroid_prep(cur, guard));
         reset_kernel<<<grid1d(k_pad * d4 + k_pad, 256, 2048), 256, 0, s>>>(
-            sums_km, k_pad * d4, sizes32, k_pad, n_flagged, guard);
+            sums32, sizes32, acc64, k_pad * d4, k_pad, priv64, n_flagged, guard);
         KMC_TRY(check_launch("mixed_reset"));
         MixedArgs a;
         a.ximg = ximg;
@@ -842,8 +996,10 @@ struct MixedFit : PlainFit<float, I> {
         a.X = p.X;
         a.w = p.w;
         a.labels = p.labels;
-        a.sums_km = sums_km;
-        a.sizes = sizes32;
+        a.sums32 = sums32;
+        a.sizes32 = sizes32;
+        a.acc64 = acc64;
+        a.xflag = xflag;
         a.cand = cand;
         a.flagged = flagged;
         a.n_flagged = n_flagged;
@@ -856,7 +1012,9 @@ struct MixedFit : PlainFit<float, I> {
         a.d4 = d4;
         a.update = update;
         a.label64 = sizeof(I) == 8 ? 1 : 0;
-        const SmemLayout L = smem_layout(nkb, k_pad);
+        a.priv64 = priv64;
+        a.keep_p1 = keep_p1;
+        const SmemLayout L = smem_layout(nkb, k_pad, d4, priv64, keep_p1);
         auto kern = bf16 ? (nkb == 1 ? mixed_assign_kernel<1, 1> : mixed_assign_kernel<1, 2>)
                          : (nkb == 1 ? mixed_assign_kernel<0, 1> : mixed_assign_kernel<0, 2>);
         KMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -867,10 +1025,10 @@ struct MixedFit : PlainFit<float, I> {
             KMC_TRY(check_launch("mixed_assign"));
         }
         const int rblock = 256;
-        const size_t rsmem = sizeof(float) * (rblock / 32) * std::max<int64_t>(p.d, 1);
+        const size_t rsmem = sizeof(float) * (rblock / 32) * d4;
         recheck_kernel<<<(unsigned)(num_sms() * 4), rblock, rsmem, s>>>(
-            p.X, p.w, cur, this->hn, cand, flagged, n_flagged, p.n, p.d, p.k, d4, p.labels,
-            a.label64, sums_km, sizes32, update, guard);
+            xflag, ct, this->hn, p.w, cand, flagged, n_flagged, p.n, p.d, p.k, d4, p.labels,
+            a.label64, update, priv64, sums32, sizes32, acc64, k_pad, guard);
         KMC_TRY(check_launch("mixed_recheck"));
         stats_kernel<<<1, 1, 0, s>>>(n_flagged, stats, stats + 1, guard);
         return check_launch("mixed_stats");
@@ -884,8 +1042,12 @@ struct MixedFit : PlainFit<float, I> {
     int reduce_step(float *nxt) override {
         const FitParams<float, I> &p = this->prm;
         cudaStream_t s = p.stream;
-        km_to_dk_kernel<<<grid1d(p.d * p.k + p.k, 256, 4096), 256, 0, s>>>(
-            sums_km, sizes32, nxt, this->sizes, p.d, p.k, d4, this->state);
+        if (priv64)
+            km_to_dk_kernel<double><<<grid1d(p.d * p.k + p.k, 256, 4096), 256, 0, s>>>(
+                acc64, acc64 + k_pad * d4, nxt, this->sizes, p.d, p.k, d4, this->state);
+        else
+            km_to_dk_kernel<float><<<grid1d(p.d * p.k + p.k, 256, 4096), 256, 0, s>>>(
+                sums32, sizes32, nxt, this->sizes, p.d, p.k, d4, this->state);
         KMC_TRY(check_launch("km_to_dk"));
         return launch_empty_list<float, I>(this->sizes, this->empty_list, this->n_empty, p.k, s,
                                            this->state);

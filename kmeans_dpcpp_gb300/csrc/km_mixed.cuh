@@ -42,14 +42,17 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
                  : "memory");
 }
 
+// try_wait suspends the thread in hardware until the phase completes or the
+// suspend-time hint (ns) expires, so waiting warps do not spin on the issue
+// slots the working warps need.
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(1000000u)
         : "memory");
     return ok != 0;
 }
@@ -153,6 +156,18 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
     return d;
 }
 
+// Same for a K extent of 16 16-bit elements (32-byte rows): 32-byte
+// swizzle, 8-row groups of 256 bytes (stride byte offset 256), mode 6.
+__device__ __forceinline__ uint64_t desc_sw32(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(256u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)6 << 61;  // 32-byte swizzle
+    return d;
+}
+
 // Instruction descriptor, kind::f16: fp32 accumulator, A and B both fp16
 // (bf16 = 0) or both bf16 (bf16 = 1), both K-major, shape M x N.
 __host__ __device__ constexpr uint32_t idesc_f16(int bf16, int M, int N) {
@@ -164,6 +179,14 @@ __host__ __device__ constexpr uint32_t idesc_f16(int bf16, int M, int N) {
 // image whose base is 1024-byte aligned.
 __host__ __device__ constexpr uint32_t sw128_offset(uint32_t r, uint32_t k) {
     return (r >> 3) * 1024u + (r & 7u) * 128u + ((((k >> 3) ^ (r & 7u)) & 7u) << 4) +
+           (k & 7u) * 2u;
+}
+
+// Byte offset of element (r, k) (k < 16) inside a 32-byte-swizzled K-major
+// image (8-row atoms of 256 bytes; the 16-byte halves of rows 4-7 of each
+// atom are swapped), base 1024-byte aligned.
+__host__ __device__ constexpr uint32_t sw32_offset(uint32_t r, uint32_t k) {
+    return (r >> 3) * 256u + (r & 7u) * 32u + ((((k >> 3) ^ ((r & 7u) >> 2)) & 1u) << 4) +
            (k & 7u) * 2u;
 }
 
