@@ -2,9 +2,11 @@
 //
 // The assignment needs, for each sample x and centroid c_j, the reference's
 // pseudo-distance D_j = half_norm[j] - x.c_j (src/device_functions.hpp:
-// 106-162).  Here the contraction x.c_j runs on the tensor cores with fp16
-// (or bf16) operands and fp32 accumulation; the score s_j = x.c_j - hn_j is
-// formed in fp32 with the reference's exact half norms.  For every sample the
+// 106-162).  Here the score s_j = sigma^2 (x.c_j - hn_j) is produced entirely
+// by the tensor cores: the contraction over the features runs with fp16 (or
+// bf16) operands and fp32 accumulation, and one more K=16 MMA per chunk adds
+// -hn_j, split into three 16-bit parts against constant columns
+// (-2^10, -1, -2^-10), so TMEM holds finished scores.  For every sample the
 // epilogue finds the best score M and an exact bound on the runner-up R
 // without sorting (see "runner-up" below).  A sample whose margin M - R
 // exceeds twice its error bound E_i is certified: no rounding of the
@@ -18,13 +20,15 @@
 // scaled by a global power of two sigma, eta = 2^-25 the fp16 subnormal
 // half-spacing, d features):
 //   E_i = ||x_i||_2 * Cmax * kappa + (eta/sigma)(1+u)(||x_i||_1 + C1max)
-//         + d (eta/sigma)^2 + 2^-23 * 1.01 * Hmax
+//         + d (eta/sigma)^2 + Hmax (u^3 + 2^-16) + 2^-13 / sigma^2
 //   kappa = 2u + u^2 + 2^-16 + (d + 4) 2^-23
 // with Cmax = max_j ||c_j||_2, C1max = max_j ||c_j||_1, Hmax = max_j |hn_j|.
-// It covers operand rounding (2u + u^2 per product), tensor-core fp32
-// accumulation (<= 2^-17 relative, allowing truncation), the fp32 score
-// rounding, and the reference's sequential fp32 dot (d 2^-24) and final
-// subtraction.  All norms are rounded up.
+// It covers operand rounding (2u + u^2 per product), the three-part split of
+// the half norms (u^3, plus subnormal parts), tensor-core fp32 accumulation
+// (<= 2^-17 relative to the sum of magnitudes, allowing truncation), and the
+// reference's sequential fp32 dot (d 2^-24) and final subtraction.  All norms
+// are rounded up.  sigma keeps |x sigma| <= 2^14 and sigma^2 * hn <= 2^25 so
+// every 16-bit part is finite.
 //
 // Runner-up without sorting: per sample, P1[s] = max over 32-column
 // sub-chunk s and P2[t] = max over columns j = t (mod 32).  Two distinct
@@ -38,7 +42,7 @@
 //   warp 0      bulk copies: the centroid image once, X tiles into a 4-stage ring
 //   warp 1      TMEM allocation; one thread issues tcgen05.mma (M=128, N=256,
 //               K=16) into two 256-column TMEM accumulators
-//   warps 2-9   epilogue: tcgen05.ld, scores, P1/P2, certification, labels
+//   warps 2-9   epilogue: tcgen05.ld of score pairs, P1/P2, certification, labels
 //   warps 10-13 update: w*x of certified samples into the cluster sums
 //               (red.global.add.v4.f32, cluster-major layout)
 // Samples that fail certification are accumulated by the recheck kernel.
@@ -59,7 +63,7 @@ using namespace tc;
 constexpr int kTileM = 128;
 constexpr int kChunkN = 256;
 constexpr int kMaxStages = 4;
-__host__ __device__ constexpr int stages_for(int nkb) { return nkb == 1 ? 4 : 2; }
+constexpr uint32_t kNormRowBytes = 32;  // K=16 block holding the half-norm parts
 constexpr int kEpiWarps = 8;
 constexpr int kUpdWarps = 4;
 constexpr int kThreadsMixed = 32 * (2 + kEpiWarps + kUpdWarps);
@@ -68,19 +72,19 @@ constexpr uint32_t kTileBytes = kTileM * 128;  // one 64-wide K block of a tile
 constexpr size_t kSmemLimit = 232448;
 
 struct MixedConsts {
-    float inv_s2;   // 1 / sigma^2
+    float s2;       // sigma^2 (scores in TMEM are sigma^2 (x.c - hn))
     float alpha;    // E_i = nx_i * alpha + n1_i * beta1 + beta0
     float beta1;
     float beta0;
     float sigma;
     unsigned int xmax_bits;  // max |x| (fp32 bits)
-    int pad0, pad1;
+    int overflow;            // an operand left the 16-bit range this pass
+    int pad1;
 };
 
 struct MixedArgs {
     const uint8_t *ximg;
     const uint8_t *cimg;
-    const float *hn;
     const float *nx;
     const float *n1;
     const MixedConsts *consts;
@@ -101,25 +105,34 @@ struct MixedArgs {
     int label64;
     int priv64;        // accumulate in fp64 in shared memory, flushed once per CTA
     int keep_p1;       // exact sub-chunk hot masks from shared memory
+    int stages;        // depth of the X-tile ring
 };
 
 struct SmemLayout {
-    size_t c, x, hn, xch, lab, bar, priv, p1, total;
+    size_t c, hnb, aon, x, xch, lab, bar, priv, p1, total;
 };
 
-// p1: sub-chunk maxima of every epilogue thread (k_pad / 64 floats each), kept
-// so that uncertified samples get exact candidate masks.
-__host__ __device__ inline SmemLayout smem_layout(int nkb, int64_t k_pad, int64_t d4 = 0,
-                                                  int priv64 = 0, int keep_p1 = 0) {
+// c:    centroid image, NKB blocks of k_pad x 128 bytes (128-byte swizzle)
+// hnb:  half-norm parts, k_pad x 32 bytes (32-byte swizzle); c and hnb are
+//       one contiguous copy of the global centroid image
+// aon:  constant A block (128 x 32 bytes): columns 0..2 = -2^10, -1, -2^-10
+// x:    X-tile ring (stages x NKB x 16 KB)
+// p1:   sub-chunk maxima of every epilogue thread, [sub-chunk][thread], kept
+//       so that uncertified samples get exact candidate masks
+__host__ __device__ inline SmemLayout smem_layout(int nkb, int64_t k_pad, int64_t d4,
+                                                  int priv64, int keep_p1, int stages) {
     SmemLayout L;
     size_t off = 0;
     L.c = off;
     off += (size_t)nkb * k_pad * 128;
+    L.hnb = off;
+    off += (size_t)k_pad * kNormRowBytes;
+    off = (off + 1023) & ~size_t(1023);
+    L.aon = off;
+    off += (size_t)kTileM * kNormRowBytes;
     off = (off + 1023) & ~size_t(1023);
     L.x = off;
-    off += (size_t)stages_for(nkb) * nkb * kTileBytes;
-    L.hn = off;
-    off += sizeof(float) * k_pad;
+    off += (size_t)stages * nkb * kTileBytes;
     L.xch = off;
     off += sizeof(float) * 2 * 2 * kTileM * 3;
     L.lab = off;
@@ -136,10 +149,47 @@ __host__ __device__ inline SmemLayout smem_layout(int nkb, int64_t k_pad, int64_
     return L;
 }
 
+// Bytes of the global centroid image (128-byte-swizzled blocks + norm parts).
+__host__ __device__ inline size_t cimg_bytes(int nkb, int64_t k_pad) {
+    return (size_t)nkb * k_pad * 128 + (size_t)k_pad * kNormRowBytes;
+}
+
 __device__ __forceinline__ float max3f(float a, float b, float c) {
     float r;
     asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
     return r;
+}
+
+__device__ __forceinline__ float u2f(uint32_t v) { return __uint_as_float(v); }
+
+// Maximum of 32 scores (16 three-input max operations).
+__device__ __forceinline__ float max32(const uint32_t (&r)[32]) {
+    float m[11];
+#pragma unroll
+    for (int u = 0; u < 10; ++u) m[u] = max3f(u2f(r[3 * u]), u2f(r[3 * u + 1]), u2f(r[3 * u + 2]));
+    m[10] = fmaxf(u2f(r[30]), u2f(r[31]));
+    const float a = max3f(m[0], m[1], m[2]);
+    const float b = max3f(m[3], m[4], m[5]);
+    const float c = max3f(m[6], m[7], m[8]);
+    return fmaxf(max3f(a, b, c), fmaxf(m[9], m[10]));
+}
+
+// tcgen05.ld writes its registers asynchronously; after tcgen05.wait::ld the
+// empty asm statements (ordered after the wait like every volatile asm) make
+// each later use of the registers depend on the wait.
+__device__ __forceinline__ void tmem_ld_wait_regs(uint32_t (&r0)[32], uint32_t (&r1)[32]) {
+    tmem_ld_wait();
+#pragma unroll
+    for (int t = 0; t < 32; ++t) asm volatile("" : "+r"(r0[t]), "+r"(r1[t]));
+}
+
+// Columns at or beyond k (padding of the last chunk) never win.
+__device__ __forceinline__ void mask_tail(uint32_t (&r)[32], int64_t j0, int64_t k) {
+    if (j0 + 32 > k) {
+#pragma unroll
+        for (int t = 0; t < 32; ++t)
+            if (j0 + t >= k) r[t] = __float_as_uint(-pos_inf<float>());
+    }
 }
 
 __device__ __forceinline__ bool epi_any(bool v) {
@@ -156,30 +206,45 @@ __device__ __forceinline__ bool epi_any(bool v) {
     return r != 0;
 }
 
-__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
-
 // Position of the n-th (0-based) set bit of m (m has more than n set bits).
 __device__ __forceinline__ int nth_set_bit(uint32_t m, int n) {
     for (int q = 0; q < n; ++q) m &= m - 1u;
     return __ffs(m) - 1;
 }
 
+template <int BF16>
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+    if (BF16) {
+        __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&h);
+    } else {
+        __half2 h = __floats2half2_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&h);
+    }
+}
+
+// Constant columns of the half-norm block: the score receives
+// -(c0 h0 + c1 h1 + c2 h2) with (h0, h1, h2) the 16-bit parts of sigma^2 hn.
+__host__ __device__ constexpr float norm_coef(int bf16, int part) {
+    return bf16 ? -1.f : (part == 0 ? -1024.f : (part == 1 ? -1.f : -0x1p-10f));
+}
+
 template <int BF16, int NKB>
 __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArgs a) {
-    constexpr int kStages = stages_for(NKB);
     if (a.guard != nullptr && *reinterpret_cast<const volatile int *>(&a.guard->done)) return;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
-    // the 128-byte swizzle is a function of absolute shared-memory address
-    // bits, so every operand image starts on a 1024-byte boundary
+    // the swizzles are functions of absolute shared-memory address bits, so
+    // every operand image starts on a 1024-byte boundary
     uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     const int64_t k_pad = a.k_pad;
     const int nch = (int)(k_pad / kChunkN);
-    const SmemLayout L = smem_layout(NKB, k_pad, a.d4, a.priv64, a.keep_p1);
+    const int stages = a.stages;
+    const SmemLayout L = smem_layout(NKB, k_pad, a.d4, a.priv64, a.keep_p1, stages);
     uint8_t *cimg_s = smem + L.c;
+    uint8_t *aon_s = smem + L.aon;
     double *priv = reinterpret_cast<double *>(smem + L.priv);
     float *p1s = reinterpret_cast<float *>(smem + L.p1);
     uint8_t *xring = smem + L.x;
-    float *hn_s = reinterpret_cast<float *>(smem + L.hn);
     float *xch = reinterpret_cast<float *>(smem + L.xch);
     int *lab_s = reinterpret_cast<int *>(smem + L.lab);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.bar);
@@ -191,10 +256,10 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t n = a.n, k = a.k;
     const int64_t ntiles = ceil_div<int64_t>(n, kTileM);
-    const uint32_t cbytes = (uint32_t)(NKB * k_pad * 128);
+    const uint32_t cbytes = (uint32_t)cimg_bytes(NKB, k_pad);
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) {
+        for (int s = 0; s < stages; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
@@ -209,8 +274,16 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
         *err = 0;
         fence_barrier_init();
     }
-    for (int64_t j = threadIdx.x; j < k_pad; j += blockDim.x)
-        hn_s[j] = (j < k) ? a.hn[j] : pos_inf<float>();
+    // constant A block of the half-norm MMA: row r = (c0, c1, c2, 0, ..., 0)
+    for (int t = threadIdx.x; t < 2 * kTileM; t += blockDim.x) {
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if ((t & 1) == 0) {
+            v.x = pack2<BF16>(norm_coef(BF16, 0), norm_coef(BF16, 1));
+            v.y = pack2<BF16>(norm_coef(BF16, 2), 0.f);
+        }
+        *reinterpret_cast<uint4 *>(aon_s + sw32_offset((uint32_t)(t >> 1), (uint32_t)(t & 1) * 8)) = v;
+    }
+    fence_proxy_async();  // generic-proxy writes -> tensor-core operand reads
     if (a.priv64)
         for (int64_t e = threadIdx.x; e < k_pad * a.d4 + k_pad; e += blockDim.x) priv[e] = 0.0;
     if (warp == 1) {
@@ -230,25 +303,23 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
             for (uint32_t off = 0; off < cbytes; off += 32768u)
                 bulk_g2s(cimg_s + off, a.cimg + off, min(32768u, cbytes - off), cbar);
             int s = 0;
-            uint32_t ph = 0;
-            int issued[kMaxStages] = {0, 0, 0, 0};
-            uint32_t last_ph[kMaxStages] = {0, 0, 0, 0};
+            uint32_t ph = 0, issued = 0u, last_ph = 0u;
             for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
                 if (!mbar_wait(&empty[s], ph ^ 1u, err)) break;
                 mbar_arrive_expect_tx(&full[s], NKB * kTileBytes);
                 bulk_g2s(xring + (size_t)s * NKB * kTileBytes,
                          a.ximg + (size_t)tile * NKB * kTileBytes, NKB * kTileBytes, &full[s]);
-                issued[s] = 1;
-                last_ph[s] = ph;
-                if (++s == kStages) {
+                issued |= 1u << s;
+                last_ph = (last_ph & ~(1u << s)) | (ph << s);
+                if (++s == stages) {
                     s = 0;
                     ph ^= 1u;
                 }
             }
             // never leave a copy in flight into this CTA's shared memory
             mbar_wait(cbar, 0, err);
-            for (int q = 0; q < kStages; ++q)
-                if (issued[q]) mbar_wait(&full[q], last_ph[q], err);
+            for (int q = 0; q < stages; ++q)
+                if ((issued >> q) & 1u) mbar_wait(&full[q], (last_ph >> q) & 1u, err);
         }
         __syncwarp();
     } else if (warp == 1) {
@@ -256,6 +327,8 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
         if (lane == 0) {
             const uint32_t idesc = idesc_f16(BF16, kTileM, kChunkN);
             const uint32_t cbase = smem_u32(cimg_s);
+            const uint32_t hbase = cbase + (uint32_t)(NKB * k_pad * 128);
+            const uint64_t adesc_norm = desc_sw32(smem_u32(aon_s));
             bool ok = mbar_wait(cbar, 0, err);
             int s = 0;
             uint32_t ph = 0, cnt = 0;
@@ -280,11 +353,14 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                                                            (uint32_t)(c * kChunkN * 128) + kk * 32);
                             mma_f16(dt, ad, bd, idesc, (kb | kk) != 0 ? 1u : 0u);
                         }
+                    // - sigma^2 hn_j for the 256 columns of this chunk
+                    mma_f16(dt, adesc_norm,
+                            desc_sw32(hbase + (uint32_t)(c * kChunkN) * kNormRowBytes), idesc, 1u);
                     mma_commit(&tfull[b]);
                     ++cnt;
                 }
                 mma_commit(&empty[s]);
-                if (++s == kStages) {
+                if (++s == stages) {
                     s = 0;
                     ph ^= 1u;
                 }
@@ -304,7 +380,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
         uint32_t cnt = 0;
         int tl = 0;
         const int nsc_h = (int)(k_pad / 64);  // sub-chunks per column half
-        float *my_p1 = p1s + (size_t)(ew * 32 + lane) * nsc_h;
+        float *my_p1 = p1s + ew * 32 + lane;   // [sub-chunk][256 threads]
         // per-sample norms of the next tile are loaded one tile ahead
         float nx_next = 0.f, n1_next = 0.f;
         {
@@ -318,7 +394,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
             const int64_t i = tile * kTileM + row;
             float E2 = 0.f;
             if (i < n) {
-                float e = fmaf(nx_next, cst.alpha, fmaf(n1_next, cst.beta1, cst.beta0));
+                const float e = fmaf(nx_next, cst.alpha, fmaf(n1_next, cst.beta1, cst.beta0));
                 E2 = 2.f * e * 1.000001f;
             }
             {
@@ -335,6 +411,19 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
             int srun = 0;
             uint32_t hot1 = 0u;
             bool bad = false;
+            // sub-chunk maximum m of sub-chunk sidx: running best / runner-up
+            auto record = [&](float m, int sidx) {
+                R1 = fmaxf(R1, fminf(Mrun, m));
+                srun = (m > Mrun) ? sidx : srun;
+                Mrun = fmaxf(Mrun, m);
+                if (a.keep_p1) {
+                    my_p1[sidx * 256] = m;
+                } else if (m >= Mrun - E2) {
+                    // superset of the final hot sub-chunks: the final
+                    // threshold M - E2 is at least Mrun - E2
+                    hot1 |= 1u << sidx;
+                }
+            };
             for (int c = 0; c < nch; ++c) {
                 const uint32_t b = cnt & 1u, bph = (cnt >> 1) & 1u;
                 if (!mbar_wait(&tfull[b], bph, err)) bad = true;
@@ -344,64 +433,38 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                     break;
                 }
                 tc_fence_after();
-                const uint32_t cbase = tmem + lane_addr + b * kChunkN + h * 128;
-                // one 32-column sub-chunk: scores, class maxima, sub-chunk maximum
-                auto process = [&](const uint32_t (&r)[32], int qq) {
-                    const int j0 = c * kChunkN + h * 128 + qq * 32;
-                    const float4 *hv = reinterpret_cast<const float4 *>(hn_s + j0);
-                    float v[32];
-#pragma unroll
-                    for (int t4 = 0; t4 < 8; ++t4) {
-                        const float4 hh = hv[t4];
-                        v[4 * t4 + 0] = fmaf(__uint_as_float(r[4 * t4 + 0]), cst.inv_s2, -hh.x);
-                        v[4 * t4 + 1] = fmaf(__uint_as_float(r[4 * t4 + 1]), cst.inv_s2, -hh.y);
-                        v[4 * t4 + 2] = fmaf(__uint_as_float(r[4 * t4 + 2]), cst.inv_s2, -hh.z);
-                        v[4 * t4 + 3] = fmaf(__uint_as_float(r[4 * t4 + 3]), cst.inv_s2, -hh.w);
-                    }
-#pragma unroll
-                    for (int t = 0; t < 32; ++t) P2[t] = fmaxf(P2[t], v[t]);
-                    float m11[11];
-#pragma unroll
-                    for (int u = 0; u < 10; ++u) m11[u] = max3f(v[3 * u], v[3 * u + 1], v[3 * u + 2]);
-                    m11[10] = fmaxf(v[30], v[31]);
-                    const float m4a = max3f(m11[0], m11[1], m11[2]);
-                    const float m4b = max3f(m11[3], m11[4], m11[5]);
-                    const float m4c = max3f(m11[6], m11[7], m11[8]);
-                    const float m4d = fmaxf(m11[9], m11[10]);
-                    const float m = fmaxf(max3f(m4a, m4b, m4c), m4d);
-                    const int sidx = c * 4 + qq;
-                    if (m > Mrun) {
-                        R1 = Mrun;
-                        Mrun = m;
-                        srun = sidx;
-                    } else if (m > R1) {
-                        R1 = m;
-                    }
-                    if (a.keep_p1) {
-                        my_p1[sidx] = m;
-                    } else {
-                        // superset of the final hot sub-chunks: the final
-                        // threshold M - 2E is at least Mrun - 2E
-                        if (m >= Mrun - E2) hot1 |= 1u << sidx;
-                    }
-                };
-                // double-buffered TMEM loads: the next sub-chunk is in flight
-                // while the current one is processed
+                const uint32_t cb = tmem + lane_addr + b * kChunkN + h * 128;
+                const int64_t j0 = (int64_t)c * kChunkN + h * 128;
                 uint32_t ra[32], rb[32];
-                tmem_ld32(cbase + 0, ra);
-                tmem_ld_wait();
-                tmem_ld32(cbase + 32, rb);
-                process(ra, 0);
-                tmem_ld_wait();
-                tmem_ld32(cbase + 64, ra);
-                process(rb, 1);
-                tmem_ld_wait();
-                tmem_ld32(cbase + 96, rb);
-                process(ra, 2);
-                tmem_ld_wait();
+                // sub-chunks 0 and 1
+                tmem_ld32(cb, ra);
+                tmem_ld32(cb + 32, rb);
+                tmem_ld_wait_regs(ra, rb);
+                mask_tail(ra, j0, k);
+                mask_tail(rb, j0 + 32, k);
+#pragma unroll
+                for (int t = 0; t < 32; ++t) P2[t] = max3f(P2[t], u2f(ra[t]), u2f(rb[t]));
+                const float m0 = max32(ra);
+                // the loads below reuse ra / rb: finish every read of them first
+#pragma unroll
+                for (int t = 0; t < 32; ++t) asm volatile("" : "+f"(P2[t]));
+                asm volatile("" ::"f"(m0));
+                tmem_ld32(cb + 64, ra);
+                const float m1 = max32(rb);
+                asm volatile("" ::"f"(m1));
+                tmem_ld32(cb + 96, rb);
+                record(m0, 4 * c);
+                record(m1, 4 * c + 1);
+                // sub-chunks 2 and 3
+                tmem_ld_wait_regs(ra, rb);
                 tc_fence_before();
                 mbar_arrive(&tempty[b]);  // the accumulator may be overwritten now
-                process(rb, 3);
+                mask_tail(ra, j0 + 64, k);
+                mask_tail(rb, j0 + 96, k);
+#pragma unroll
+                for (int t = 0; t < 32; ++t) P2[t] = max3f(P2[t], u2f(ra[t]), u2f(rb[t]));
+                record(max32(ra), 4 * c + 2);
+                record(max32(rb), 4 * c + 3);
                 ++cnt;
             }
 
@@ -410,13 +473,9 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
             int t2 = 0;
 #pragma unroll
             for (int t = 0; t < 32; ++t) {
-                if (P2[t] > M2) {
-                    R2 = M2;
-                    M2 = P2[t];
-                    t2 = t;
-                } else if (P2[t] > R2) {
-                    R2 = P2[t];
-                }
+                R2 = fmaxf(R2, fminf(M2, P2[t]));
+                t2 = (P2[t] > M2) ? t : t2;
+                M2 = fmaxf(M2, P2[t]);
             }
             const float Mh = Mrun;
             const float Rh = fmaxf(R1, R2);
@@ -457,7 +516,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                     if (a.keep_p1) {
                         hot1 = 0u;
                         for (int sc = 0; sc < nsc_h; ++sc)
-                            if (my_p1[sc] >= thr) hot1 |= 1u << sc;
+                            if (my_p1[sc * 256] >= thr) hot1 |= 1u << sc;
                     }
                     uint32_t *cw = reinterpret_cast<uint32_t *>(a.cand + i);
                     cw[h] = hot1;
@@ -580,27 +639,23 @@ __global__ void absmax_kernel(const float *X, int64_t count, unsigned int *out_b
     if ((threadIdx.x & 31) == 0 && m == m) atomicMax(out_bits, __float_as_uint(m));
 }
 
-// sigma = 2^-e keeps the largest |x * sigma| at or below 2^14 (fp16 range);
-// bf16 shares fp32's exponent range and is never scaled.
-__global__ void sigma_kernel(MixedConsts *c, int bf16) {
-    float xmax = __uint_as_float(c->xmax_bits);
-    float sigma = 1.f;
-    if (!bf16) {
-        while (xmax * sigma > 16384.f && sigma > 1e-30f) sigma *= 0.5f;
+// fp16 operands: sigma is the largest power of two in [2^-60, 2^60] with
+// max|x| sigma <= 2^14 and sigma^2 d max|x|^2 / 2 <= 2^25, so that every
+// scaled sample, every scaled centroid inside the data's range and the
+// largest part of sigma^2 hn stay finite in fp16 with room to spare.  bf16
+// shares fp32's exponent range and is never scaled.
+__global__ void sigma_kernel(MixedConsts *c, int bf16, int64_t d) {
+    const double xmax = (double)__uint_as_float(c->xmax_bits);
+    double sigma = 1.0;
+    if (!bf16 && xmax > 0.0 && xmax < 1e300) {
+        const double hx = 0.5 * (double)d * xmax * xmax;
+        auto fits = [&](double s) { return xmax * s <= 0x1p14 && s * s * hx <= 0x1p25; };
+        while (sigma < 0x1p60 && fits(sigma * 2.0)) sigma *= 2.0;
+        while (sigma > 0x1p-60 && !fits(sigma)) sigma *= 0.5;
     }
-    c->sigma = sigma;
-    c->inv_s2 = 1.f / (sigma * sigma);
-}
-
-template <int BF16>
-__device__ __forceinline__ uint32_t pack2(float a, float b) {
-    if (BF16) {
-        __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-        return *reinterpret_cast<uint32_t *>(&h);
-    } else {
-        __half2 h = __floats2half2_rn(a, b);
-        return *reinterpret_cast<uint32_t *>(&h);
-    }
+    c->sigma = (float)sigma;
+    c->s2 = (float)(sigma * sigma);
+    c->overflow = 0;
 }
 
 // One thread per sample row (including the zero rows that pad the last
@@ -642,16 +697,39 @@ __global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int nkb, in
     }
 }
 
-// Centroid image (rows j < k_pad, zero padding) and per-centroid norms.
+// Round to the 16-bit operand type and back (exact in fp32).
 template <int BF16>
-__global__ void c_image_kernel(const float *C, int64_t d, int64_t k, int64_t k_pad, int nkb,
-                               const MixedConsts *c, uint8_t *img, float *cn2, float *cn1,
-                               float *ct, int64_t d4, const LoopState *guard) {
+__device__ __forceinline__ float round16(float v) {
+    if (BF16) return __bfloat162float(__float2bfloat16_rn(v));
+    return __half2float(__float2half_rn(v));
+}
+
+// Largest finite operand value: fp16 65504, bf16 (1 - 2^-8) 2^128.
+template <int BF16>
+__device__ __forceinline__ float max16() {
+    return BF16 ? 3.3895313892515355e38f : 65504.f;
+}
+
+// Centroid image (rows j < k_pad, zero padding), the half-norm block and the
+// per-centroid norms.  Row j of the half-norm block holds (h0, h1, h2) with
+//   c0 h0 + c1 h1 + c2 h2 = -sigma^2 hn_j   (c = norm_coef)
+// up to sigma^2 |hn_j| u^3 (u = 2^-11 fp16, 2^-8 bf16; plus 2^-35 for fp16
+// subnormal parts): h0 is the rounded leading part and each following part
+// the rounded remainder, formed exactly in fp64.  A value that would leave the
+// operand range is clamped and raises consts->overflow, which disables
+// certification for the pass (every sample is then re-evaluated exactly).
+template <int BF16>
+__global__ void c_image_kernel(const float *C, const float *hn, int64_t d, int64_t k,
+                               int64_t k_pad, int nkb, MixedConsts *c, uint8_t *img, float *cn2,
+                               float *cn1, float *ct, int64_t d4, const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
     const float sigma = c->sigma;
+    const double s2 = (double)sigma * (double)sigma;
+    const float lim = max16<BF16>();
+    bool ovf = false;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < k_pad;
          j += (int64_t)gridDim.x * blockDim.x) {
-        double s2 = 0.0, s1 = 0.0;
+        double q2 = 0.0, q1 = 0.0;
         for (int kb = 0; kb < nkb; ++kb) {
             uint8_t *base = img + (size_t)kb * k_pad * 128;
             for (int ch = 0; ch < 8; ++ch) {
@@ -660,9 +738,14 @@ __global__ void c_image_kernel(const float *C, int64_t d, int64_t k, int64_t k_p
                 for (int e = 0; e < 8; ++e) {
                     const int64_t f = (int64_t)kb * 64 + ch * 8 + e;
                     const float x = (j < k && f < d) ? C[f * k + j] : 0.f;
-                    s2 += (double)x * (double)x;
-                    s1 += fabs((double)x);
-                    v[e] = x * sigma;
+                    q2 += (double)x * (double)x;
+                    q1 += fabs((double)x);
+                    float sv = x * sigma;
+                    if (!(fabsf(sv) <= lim)) {
+                        ovf = true;
+                        sv = (sv > 0.f) ? lim : ((sv < 0.f) ? -lim : 0.f);
+                    }
+                    v[e] = sv;
                     if (f < d4) ct[j * d4 + f] = x;
                 }
                 uint4 pk;
@@ -673,14 +756,38 @@ __global__ void c_image_kernel(const float *C, int64_t d, int64_t k, int64_t k_p
                 *reinterpret_cast<uint4 *>(base + sw128_offset((uint32_t)j, (uint32_t)ch * 8)) = pk;
             }
         }
+        float h0 = 0.f, h1 = 0.f, h2 = 0.f;
         if (j < k) {
-            cn2[j] = __double2float_ru(sqrt(s2) * (1.0 + 1e-12));
-            cn1[j] = __double2float_ru(s1 * (1.0 + 1e-12));
+            const double H = (double)hn[j] * s2;
+            const double c0 = -(double)norm_coef(BF16, 0), c1 = -(double)norm_coef(BF16, 1),
+                         c2 = -(double)norm_coef(BF16, 2);
+            h0 = round16<BF16>((float)(H / c0));
+            if (!(fabsf(h0) <= lim)) {
+                ovf = true;
+                h0 = (H > 0.0) ? lim : -lim;
+            }
+            const double r1 = H - c0 * (double)h0;
+            h1 = round16<BF16>((float)(r1 / c1));
+            const double r2 = r1 - c1 * (double)h1;
+            h2 = round16<BF16>((float)(r2 / c2));
+            if (!(fabsf(h1) <= lim) || !(fabsf(h2) <= lim)) {
+                ovf = true;
+                h1 = 0.f;
+                h2 = 0.f;
+            }
+            cn2[j] = __double2float_ru(sqrt(q2) * (1.0 + 1e-12));
+            cn1[j] = __double2float_ru(q1 * (1.0 + 1e-12));
         }
+        uint8_t *nb = img + (size_t)nkb * k_pad * 128;
+        uint4 p0 = make_uint4(pack2<BF16>(h0, h1), pack2<BF16>(h2, 0.f), 0u, 0u);
+        *reinterpret_cast<uint4 *>(nb + sw32_offset((uint32_t)j, 0)) = p0;
+        *reinterpret_cast<uint4 *>(nb + sw32_offset((uint32_t)j, 8)) = make_uint4(0u, 0u, 0u, 0u);
     }
+    if (ovf) atomicOr(&c->overflow, 1);
 }
 
-// Per-iteration bound constants (one block).
+// Per-iteration bound constants (one block), in the scaled units of the
+// scores (sigma^2).  Resets the overflow flag raised by c_image_kernel.
 __global__ void bound_kernel(const float *cn2, const float *cn1, const float *hn, int64_t d,
                              int64_t k, int bf16, MixedConsts *c, const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
@@ -709,18 +816,22 @@ __global__ void bound_kernel(const float *cn2, const float *cn1, const float *hn
             m1 = fmaxf(m1, sh[1][w]);
             mh = fmaxf(mh, sh[2][w]);
         }
-        m2 = fmaxf(m2, sh[0][0]);
-        m1 = fmaxf(m1, sh[1][0]);
-        mh = fmaxf(mh, sh[2][0]);
+        const double sigma = (double)c->sigma, s2 = sigma * sigma;
         const double u = bf16 ? 0x1p-8 : 0x1p-11;
-        const double eta = (bf16 ? 0x1p-134 : 0x1p-25) / (double)c->sigma;
+        // half-spacing of the operand type's subnormals (bf16: its smallest
+        // normal, in case the tensor cores flush bf16 subnormals)
+        const double eta = (bf16 ? 0x1p-126 : 0x1p-25) / sigma;
         const double kappa = 2 * u + u * u + 0x1p-16 + (double)(d + 4) * 0x1p-23;
         const double alpha = (double)m2 * kappa;
         const double beta1 = eta * (1 + u);
-        const double beta0 = beta1 * (double)m1 + (double)d * eta * eta + 0x1p-23 * 1.01 * mh;
-        c->alpha = __double2float_ru(alpha * (1 + 1e-6));
-        c->beta1 = __double2float_ru(beta1 * (1 + 1e-6));
-        c->beta0 = __double2float_ru(beta0 * (1 + 1e-6) + 1e-37);
+        const double hfloor = (bf16 ? 0x1p-126 : 0x1p-34) / s2;
+        const double beta0 = beta1 * (double)m1 + (double)d * eta * eta +
+                             (double)mh * (u * u * u + 0x1p-16 + 0x1p-23) + hfloor;
+        c->alpha = __double2float_ru(alpha * s2 * (1 + 1e-6));
+        c->beta1 = __double2float_ru(beta1 * s2 * (1 + 1e-6));
+        c->beta0 = c->overflow ? pos_inf<float>()
+                               : __double2float_ru(beta0 * s2 * (1 + 1e-6) + 1e-37);
+        c->overflow = 0;
     }
 }
 
@@ -874,6 +985,7 @@ struct MixedFit : PlainFit<float, I> {
     int nkb = 1;
     int priv64 = 0;
     int keep_p1 = 0;
+    int stages = 2;
     int64_t k_pad = 0, d4 = 0, ntiles = 0;
     Scratch mws;
     uint8_t *ximg = nullptr, *cimg = nullptr;
@@ -890,7 +1002,8 @@ struct MixedFit : PlainFit<float, I> {
         const int nk = (int)ceil_div<int64_t>(std::max<int64_t>(d, 1), 64);
         const int64_t kp = ceil_div<int64_t>(std::max<int64_t>(k, 1), kChunkN) * kChunkN;
         if (nk > 2 || kp > kMaxKPad) return false;
-        return smem_layout(nk, kp).total <= kSmemLimit;
+        const int64_t dd = ceil_div<int64_t>(std::max<int64_t>(d, 1), 4) * 4;
+        return smem_layout(nk, kp, dd, 0, 0, 2).total <= kSmemLimit;
     }
 
     int init_mixed(int form) {
@@ -901,9 +1014,24 @@ struct MixedFit : PlainFit<float, I> {
         k_pad = ceil_div<int64_t>(p.k, kChunkN) * kChunkN;
         d4 = ceil_div<int64_t>(std::max<int64_t>(p.d, 1), 4) * 4;
         ntiles = ceil_div<int64_t>(p.n, kTileM);
-        // float64 sums in shared memory when they fit next to the operands
-        priv64 = smem_layout(nkb, k_pad, d4, 1).total <= kSmemLimit ? 1 : 0;
-        keep_p1 = smem_layout(nkb, k_pad, d4, priv64, 1).total <= kSmemLimit ? 1 : 0;
+        // shared memory, in order of preference: float64 cluster sums (they
+        // keep the trajectory close to the float64 reference), then the
+        // deepest X ring, then the exact sub-chunk maxima
+        static const int kChoices[6][2] = {{4, 1}, {3, 1}, {4, 0}, {3, 0}, {2, 1}, {2, 0}};
+        bool found = false;
+        for (int pv = 1; pv >= 0 && !found; --pv)
+            for (int q = 0; q < 6 && !found; ++q)
+                if (smem_layout(nkb, k_pad, d4, pv, kChoices[q][1], kChoices[q][0]).total <=
+                    kSmemLimit) {
+                    priv64 = pv;
+                    stages = kChoices[q][0];
+                    keep_p1 = kChoices[q][1];
+                    found = true;
+                }
+        if (!found) {
+            set_error("mixed form: operands do not fit in shared memory");
+            return KMC_ERR_UNSUPPORTED;
+        }
         size_t off = 0;
         auto take = [&](size_t bytes) {
             size_t o = off;
@@ -911,7 +1039,7 @@ struct MixedFit : PlainFit<float, I> {
             return o;
         };
         const size_t o_x = take((size_t)std::max<int64_t>(ntiles, 1) * nkb * kTileBytes);
-        const size_t o_c = take((size_t)nkb * k_pad * 128);
+        const size_t o_c = take(cimg_bytes(nkb, k_pad));
         const size_t o_ct = take(sizeof(float) * k_pad * d4);
         const size_t o_nx = take(sizeof(float) * p.n);
         const size_t o_n1 = take(sizeof(float) * p.n);
@@ -951,7 +1079,7 @@ struct MixedFit : PlainFit<float, I> {
         absmax_kernel<<<grid1d(p.n * p.d, 256, 4096), 256, 0, s>>>(p.X, p.n * p.d,
                                                                     &consts->xmax_bits);
         KMC_TRY(check_launch("absmax"));
-        sigma_kernel<<<1, 1, 0, s>>>(consts, bf16);
+        sigma_kernel<<<1, 1, 0, s>>>(consts, bf16, p.d);
         KMC_TRY(check_launch("sigma"));
         const int64_t rows = ntiles * kTileM;
         if (bf16)
@@ -970,10 +1098,10 @@ struct MixedFit : PlainFit<float, I> {
         cudaStream_t s = p.stream;
         if (bf16)
             c_image_kernel<1><<<grid1d(k_pad, 128, 4096), 128, 0, s>>>(
-                cur, p.d, p.k, k_pad, nkb, consts, cimg, cn2, cn1, ct, d4, guard);
+                cur, this->hn, p.d, p.k, k_pad, nkb, consts, cimg, cn2, cn1, ct, d4, guard);
         else
             c_image_kernel<0><<<grid1d(k_pad, 128, 4096), 128, 0, s>>>(
-                cur, p.d, p.k, k_pad, nkb, consts, cimg, cn2, cn1, ct, d4, guard);
+                cur, this->hn, p.d, p.k, k_pad, nkb, consts, cimg, cn2, cn1, ct, d4, guard);
         KMC_TRY(check_launch("c_image"));
         bound_kernel<<<1, 1024, 0, s>>>(cn2, cn1, this->hn, p.d, p.k, bf16, consts, guard);
         return check_launch("bound");
@@ -989,7 +1117,6 @@ struct MixedFit : PlainFit<float, I> {
         MixedArgs a;
         a.ximg = ximg;
         a.cimg = cimg;
-        a.hn = this->hn;
         a.nx = nx;
         a.n1 = n1;
         a.consts = consts;
@@ -1014,7 +1141,8 @@ struct MixedFit : PlainFit<float, I> {
         a.label64 = sizeof(I) == 8 ? 1 : 0;
         a.priv64 = priv64;
         a.keep_p1 = keep_p1;
-        const SmemLayout L = smem_layout(nkb, k_pad, d4, priv64, keep_p1);
+        a.stages = stages;
+        const SmemLayout L = smem_layout(nkb, k_pad, d4, priv64, keep_p1, stages);
         auto kern = bf16 ? (nkb == 1 ? mixed_assign_kernel<1, 1> : mixed_assign_kernel<1, 2>)
                          : (nkb == 1 ? mixed_assign_kernel<0, 1> : mixed_assign_kernel<0, 2>);
         KMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
