@@ -149,6 +149,26 @@ int kmc_select_samples_far_from_centroid_f64_i64(int64_t n_selected,
                                                  int64_t n_samples, int64_t work_group_size,
                                                  kmc_stream_t stream);
 
+/* ---- allocation-free select_samples_far_from_centroid (float32 / int32) -----
+ * No counterpart in the reference: an extra entry point of this library for
+ * callers that must not allocate device memory during the call.  Same
+ * arguments, results and errors as kmc_select_samples_far_from_centroid_f32_i32,
+ * but its scratch is a static device array sized for n_selected <= 4096;
+ * larger n_selected is rejected with KMC_ERR_INVALID_ARGUMENT.  It makes no
+ * cudaMalloc / cudaFree or other allocating call.  Calls whose kernels overlap
+ * on the same device (other streams or host threads) race on the shared
+ * scratch.  The first call on a device looks the array up with
+ * cudaGetSymbolAddress; make it before any stream capture. */
+int kmc_select_samples_far_from_centroid_noalloc_f32_i32(int64_t n_selected,
+                                                         const float *distance_to_centroid,
+                                                         const float *threshold,
+                                                         int32_t *selected_samples_idx,
+                                                         int32_t *n_selected_gt_threshold,
+                                                         int32_t *n_selected_eq_threshold,
+                                                         int64_t n_samples,
+                                                         int64_t work_group_size,
+                                                         kmc_stream_t stream);
+
 /* ---- relocate_empty_clusters --------------------------------------------------
  * replaces py_relocate_empty_clusters (_kmeans_lloyd.cpp:443-589) ->
  * relocate_empty_clusters (src/util_kernels.hpp:392-476): threshold, select,

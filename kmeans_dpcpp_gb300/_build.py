@@ -42,6 +42,7 @@ CU_SOURCES = [
     "kernels_mixed.cu",
     "driver.cu",
     "capi.cu",
+    "noalloc.cu",
 ]
 HEADERS = ["km_common.cuh", "km_kernels.cuh", "km_fit.cuh", "km_mixed.cuh"]
 
