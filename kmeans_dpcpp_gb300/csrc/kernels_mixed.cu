@@ -37,14 +37,16 @@
 // and the winner is (argmax P1) * 32 + argmax P2 whenever the maximum is
 // unique (otherwise the margin is zero and the sample is rechecked).
 //
-// Kernel roles (one CTA of 448 threads per SM, persistent over 128-sample
-// tiles):
-//   warp 0      bulk copies: the centroid image once, X tiles into a 4-stage ring
+// Kernel roles (one CTA of 384 threads per SM, persistent over 128-sample
+// tiles; 12 warps leave 168 registers per thread, so nothing spills):
+//   warp 0      bulk copies: the centroid image once, X tiles into a 2-4 stage ring
 //   warp 1      TMEM allocation; one thread issues tcgen05.mma (M=128, N=256,
 //               K=16) into two 256-column TMEM accumulators
 //   warps 2-9   epilogue: tcgen05.ld of score pairs, P1/P2, certification, labels
-//   warps 10-13 update: w*x of certified samples into the cluster sums
-//               (red.global.add.v4.f32, cluster-major layout)
+//   warps 10-11 update: w*x of certified samples into the cluster sums
+//               (exact int64 fixed-point sums in shared memory flushed once
+//               per CTA when they fit, else red.global.add.v4.f32 into
+//               cluster-major fp32 sums)
 // Samples that fail certification are accumulated by the recheck kernel.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -62,12 +64,12 @@ using namespace tc;
 
 constexpr int kTileM = 128;
 constexpr int kChunkN = 256;
-constexpr int kMaxStages = 4;
 constexpr uint32_t kNormRowBytes = 32;  // K=16 block holding the half-norm parts
 constexpr int kEpiWarps = 8;
-constexpr int kUpdWarps = 4;
+constexpr int kUpdWarps = 2;
+constexpr int kUpdThreads = 32 * kUpdWarps;  // each handles rows u and u + 64 of a tile
 constexpr int kThreadsMixed = 32 * (2 + kEpiWarps + kUpdWarps);
-constexpr int kMaxKPad = 2048;  // sub-chunk masks are 32 bits per column half
+constexpr int kMaxChunks = 4;   // 256-column chunks per pass (k <= 1024)
 constexpr uint32_t kTileBytes = kTileM * 128;  // one 64-wide K block of a tile
 constexpr size_t kSmemLimit = 232448;
 
@@ -79,7 +81,7 @@ struct MixedConsts {
     float sigma;
     unsigned int xmax_bits;  // max |x| (fp32 bits)
     int overflow;            // an operand left the 16-bit range this pass
-    int pad1;
+    int pad;
 };
 
 struct MixedArgs {
@@ -91,10 +93,13 @@ struct MixedArgs {
     const float *X;
     const float *w;
     void *labels;
-    float *sums32;     // [k_pad][d4] fp32 cluster sums (vector-red path)
-    float *sizes32;    // [k_pad]
-    double *acc64;     // [k_pad*d4 + k_pad] fp64 sums then sizes (shared-memory path)
-    float *xflag;      // [n][d4] rows of samples sent to the exact recheck
+    // Cluster sums in n_copies private copies ([copy][k_pad*d4 + k_pad]:
+    // cluster-major sums, then sizes; CTA b uses copy b % n_copies), reduced
+    // in a fixed order afterwards.
+    float *sums32;     // fp32 copies (vector-red path)
+    double *acc64;     // fp64 copies (acc_f64 path)
+    int n_copies;
+    const float *xrow; // [n][d4] row-major fp32 copy of X (update and recheck)
     uint4 *cand;
     int *flagged;
     int *n_flagged;
@@ -103,24 +108,28 @@ struct MixedArgs {
     int64_t n, d, k, k_pad, d4;
     int update;
     int label64;
-    int priv64;        // accumulate in fp64 in shared memory, flushed once per CTA
-    int keep_p1;       // exact sub-chunk hot masks from shared memory
+    int acc_f64;       // red.global.add.f64 per feature (else red.global.add.v4.f32)
     int stages;        // depth of the X-tile ring
 };
 
 struct SmemLayout {
-    size_t c, hnb, aon, x, xch, lab, bar, priv, p1, total;
+    size_t c, hnb, aon, x, xch, lab, bar, p1, total;
 };
+
+// Sub-chunk maxima stay in registers up to two chunks; beyond that they go
+// to shared memory (registers would spill).
+__host__ __device__ constexpr bool p1_in_smem(int64_t nch) { return nch >= 3; }
 
 // c:    centroid image, NKB blocks of k_pad x 128 bytes (128-byte swizzle)
 // hnb:  half-norm parts, k_pad x 32 bytes (32-byte swizzle); c and hnb are
 //       one contiguous copy of the global centroid image
 // aon:  constant A block (128 x 32 bytes): columns 0..2 = -2^10, -1, -2^-10
 // x:    X-tile ring (stages x NKB x 16 KB)
-// p1:   sub-chunk maxima of every epilogue thread, [sub-chunk][thread], kept
-//       so that uncertified samples get exact candidate masks
+// xch:  per-row maxima of the two column halves (two tiles in flight)
+// lab:  labels / recheck slots handed to the update warps (two tiles)
+// p1:   sub-chunk maxima, [sub-chunk][256 epilogue threads] (3+ chunks)
 __host__ __device__ inline SmemLayout smem_layout(int nkb, int64_t k_pad, int64_t d4,
-                                                  int priv64, int keep_p1, int stages) {
+                                                  int stages) {
     SmemLayout L;
     size_t off = 0;
     L.c = off;
@@ -134,17 +143,15 @@ __host__ __device__ inline SmemLayout smem_layout(int nkb, int64_t k_pad, int64_
     L.x = off;
     off += (size_t)stages * nkb * kTileBytes;
     L.xch = off;
-    off += sizeof(float) * 2 * 2 * kTileM * 3;
+    off += sizeof(float) * 2 * 2 * kTileM;
     L.lab = off;
     off += sizeof(int) * 2 * kTileM;
     off = (off + 15) & ~size_t(15);
     L.bar = off;
     off += 8 * 18 + 16;
     off = (off + 15) & ~size_t(15);
-    L.priv = off;
-    if (priv64) off += sizeof(double) * (size_t)(k_pad * d4 + k_pad);
     L.p1 = off;
-    if (keep_p1) off += sizeof(float) * 32 * kEpiWarps * (size_t)(k_pad / 64);
+    if (p1_in_smem(k_pad / kChunkN)) off += sizeof(float) * 32 * kEpiWarps * (size_t)(k_pad / 64);
     L.total = off + 1024;  // slack for aligning the dynamic shared memory base
     return L;
 }
@@ -229,21 +236,18 @@ __host__ __device__ constexpr float norm_coef(int bf16, int part) {
     return bf16 ? -1.f : (part == 0 ? -1024.f : (part == 1 ? -1.f : -0x1p-10f));
 }
 
-template <int BF16, int NKB>
+template <int BF16, int NKB, int NCH>
 __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArgs a) {
     if (a.guard != nullptr && *reinterpret_cast<const volatile int *>(&a.guard->done)) return;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // the swizzles are functions of absolute shared-memory address bits, so
     // every operand image starts on a 1024-byte boundary
     uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-    const int64_t k_pad = a.k_pad;
-    const int nch = (int)(k_pad / kChunkN);
+    constexpr int64_t k_pad = (int64_t)NCH * kChunkN;
     const int stages = a.stages;
-    const SmemLayout L = smem_layout(NKB, k_pad, a.d4, a.priv64, a.keep_p1, stages);
+    const SmemLayout L = smem_layout(NKB, k_pad, a.d4, stages);
     uint8_t *cimg_s = smem + L.c;
     uint8_t *aon_s = smem + L.aon;
-    double *priv = reinterpret_cast<double *>(smem + L.priv);
-    float *p1s = reinterpret_cast<float *>(smem + L.p1);
     uint8_t *xring = smem + L.x;
     float *xch = reinterpret_cast<float *>(smem + L.xch);
     int *lab_s = reinterpret_cast<int *>(smem + L.lab);
@@ -267,7 +271,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
             mbar_init(&tfull[b], 1);
             mbar_init(&tempty[b], 32 * kEpiWarps);
             mbar_init(&ufull[b], kTileM);
-            mbar_init(&uempty[b], kTileM);
+            mbar_init(&uempty[b], kUpdThreads);
         }
         mbar_init(cbar, 1);
         mbar_init(tdone, 1);
@@ -284,8 +288,6 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
         *reinterpret_cast<uint4 *>(aon_s + sw32_offset((uint32_t)(t >> 1), (uint32_t)(t & 1) * 8)) = v;
     }
     fence_proxy_async();  // generic-proxy writes -> tensor-core operand reads
-    if (a.priv64)
-        for (int64_t e = threadIdx.x; e < k_pad * a.d4 + k_pad; e += blockDim.x) priv[e] = 0.0;
     if (warp == 1) {
         tmem_alloc(tmem_slot, 512);
         tmem_relinquish();
@@ -336,7 +338,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                 if (!mbar_wait(&full[s], ph, err)) break;
                 tc_fence_after();
                 const uint32_t xbase = smem_u32(xring + (size_t)s * NKB * kTileBytes);
-                for (int c = 0; c < nch; ++c) {
+                for (int c = 0; c < NCH; ++c) {
                     const uint32_t b = cnt & 1u, bph = (cnt >> 1) & 1u;
                     if (!mbar_wait(&tempty[b], bph ^ 1u, err)) {
                         ok = false;
@@ -372,15 +374,21 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
         __syncwarp();
     } else if (warp < 2 + kEpiWarps) {
         // ------------------------------ epilogue ------------------------------
+        // Thread (row, h) scans columns h*128 .. h*128+127 of every chunk for
+        // tile row `row`: P2[t] = max over its columns j = t (mod 32), P1[s] =
+        // max over its 32-column sub-chunk s (4 per chunk).
+        constexpr int kSub = 4 * NCH;
+        constexpr uint32_t kAll1 = (kSub == 32) ? ~0u : ((1u << kSub) - 1u);
+        constexpr bool kP1s = p1_in_smem(NCH);
+        constexpr int kChunkUnroll = kP1s ? 1 : NCH;
         const int ew = warp - 2;
+        float *my_p1 = reinterpret_cast<float *>(smem + L.p1) + (ew * 32 + lane);
         const int q = warp & 3;   // TMEM lane quadrant accessible to this warp
         const int h = ew >> 2;    // column half of each 256-wide chunk
         const int row = 32 * q + lane;
         const uint32_t lane_addr = (uint32_t)(32 * q) << 16;
         uint32_t cnt = 0;
         int tl = 0;
-        const int nsc_h = (int)(k_pad / 64);  // sub-chunks per column half
-        float *my_p1 = p1s + ew * 32 + lane;   // [sub-chunk][256 threads]
         // per-sample norms of the next tile are loaded one tile ahead
         float nx_next = 0.f, n1_next = 0.f;
         {
@@ -404,27 +412,22 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                     n1_next = a.n1[inext];
                 }
             }
-            float P2[32];
+            float P2[32], P1[kP1s ? 1 : kSub];
+            float Mh = -pos_inf<float>();
+            // sub-chunk maximum m of sub-chunk sc (register or shared copy)
+            auto put = [&](int sc, float m) {
+                Mh = fmaxf(Mh, m);
+                if constexpr (kP1s)
+                    my_p1[sc * 32 * kEpiWarps] = m;
+                else
+                    P1[sc] = m;
+            };
 #pragma unroll
             for (int t = 0; t < 32; ++t) P2[t] = -pos_inf<float>();
-            float Mrun = -pos_inf<float>(), R1 = -pos_inf<float>();
-            int srun = 0;
-            uint32_t hot1 = 0u;
             bool bad = false;
-            // sub-chunk maximum m of sub-chunk sidx: running best / runner-up
-            auto record = [&](float m, int sidx) {
-                R1 = fmaxf(R1, fminf(Mrun, m));
-                srun = (m > Mrun) ? sidx : srun;
-                Mrun = fmaxf(Mrun, m);
-                if (a.keep_p1) {
-                    my_p1[sidx * 256] = m;
-                } else if (m >= Mrun - E2) {
-                    // superset of the final hot sub-chunks: the final
-                    // threshold M - E2 is at least Mrun - E2
-                    hot1 |= 1u << sidx;
-                }
-            };
-            for (int c = 0; c < nch; ++c) {
+            // unrolled when the maxima live in registers (static indices)
+#pragma unroll kChunkUnroll
+            for (int c = 0; c < NCH; ++c) {
                 const uint32_t b = cnt & 1u, bph = (cnt >> 1) & 1u;
                 if (!mbar_wait(&tfull[b], bph, err)) bad = true;
                 // tcgen05.ld is warp-collective: re-converge after the spin-wait
@@ -440,8 +443,10 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                 tmem_ld32(cb, ra);
                 tmem_ld32(cb + 32, rb);
                 tmem_ld_wait_regs(ra, rb);
-                mask_tail(ra, j0, k);
-                mask_tail(rb, j0 + 32, k);
+                if (c == NCH - 1) {
+                    mask_tail(ra, j0, k);
+                    mask_tail(rb, j0 + 32, k);
+                }
 #pragma unroll
                 for (int t = 0; t < 32; ++t) P2[t] = max3f(P2[t], u2f(ra[t]), u2f(rb[t]));
                 const float m0 = max32(ra);
@@ -453,168 +458,158 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                 const float m1 = max32(rb);
                 asm volatile("" ::"f"(m1));
                 tmem_ld32(cb + 96, rb);
-                record(m0, 4 * c);
-                record(m1, 4 * c + 1);
+                put(4 * c, m0);
+                put(4 * c + 1, m1);
                 // sub-chunks 2 and 3
                 tmem_ld_wait_regs(ra, rb);
                 tc_fence_before();
                 mbar_arrive(&tempty[b]);  // the accumulator may be overwritten now
-                mask_tail(ra, j0 + 64, k);
-                mask_tail(rb, j0 + 96, k);
+                if (c == NCH - 1) {
+                    mask_tail(ra, j0 + 64, k);
+                    mask_tail(rb, j0 + 96, k);
+                }
 #pragma unroll
                 for (int t = 0; t < 32; ++t) P2[t] = max3f(P2[t], u2f(ra[t]), u2f(rb[t]));
-                record(max32(ra), 4 * c + 2);
-                record(max32(rb), 4 * c + 3);
+                put(4 * c + 2, max32(ra));
+                put(4 * c + 3, max32(rb));
                 ++cnt;
             }
 
-            // winner and runner-up within this column half
-            float M2 = -pos_inf<float>(), R2 = -pos_inf<float>();
-            int t2 = 0;
-#pragma unroll
-            for (int t = 0; t < 32; ++t) {
-                R2 = fmaxf(R2, fminf(M2, P2[t]));
-                t2 = (P2[t] > M2) ? t : t2;
-                M2 = fmaxf(M2, P2[t]);
-            }
-            const float Mh = Mrun;
-            const float Rh = fmaxf(R1, R2);
-            const int jh = (srun >> 2) * kChunkN + h * 128 + (srun & 3) * 32 + t2;
-            float *xb = xch + (size_t)(tl & 1) * (2 * kTileM * 3);
-            xb[(h * kTileM + row) * 3 + 0] = Mh;
-            xb[(h * kTileM + row) * 3 + 1] = __int_as_float(jh);
-            xb[(h * kTileM + row) * 3 + 2] = Rh;
+            // best score of this half, exchanged with the other half
+            float *xb = xch + (size_t)(tl & 1) * (2 * kTileM);
+            xb[h * kTileM + row] = Mh;
             // one barrier per tile: publishes the exchange and agrees on errors
             if (epi_any(bad || *err != 0)) break;
-            const float Mo = xb[((h ^ 1) * kTileM + row) * 3 + 0];
-            const int jo = __float_as_int(xb[((h ^ 1) * kTileM + row) * 3 + 1]);
-            const float Ro = xb[((h ^ 1) * kTileM + row) * 3 + 2];
-            float M, R;
-            int jw;
-            if (Mh > Mo) {
-                M = Mh;
-                jw = jh;
-                R = fmaxf(Rh, Mo);
-            } else if (Mo > Mh) {
-                M = Mo;
-                jw = jo;
-                R = fmaxf(Ro, Mh);
-            } else {
-                M = Mh;
-                jw = (h == 0) ? jh : jo;
-                R = Mh;  // tie (or both -inf): not certified
+            const float Mo = xb[(h ^ 1) * kTileM + row];
+            // Columns whose score reaches thr = M - E2 can hold the reference's
+            // winner (every score is within E2 / 2 of its exact value).  The
+            // winner is certified when exactly one column can: no column of
+            // the other half reaches thr, and exactly one sub-chunk and one
+            // class of the winning half do (two distinct columns of one
+            // sub-chunk lie in distinct classes).
+            const float thr = fmaxf(Mh, Mo) - E2;
+            const bool win = (Mh > Mo) || (Mh == Mo && h == 0);
+            uint32_t hot1 = 0u, hot2 = 0u;
+#pragma unroll
+            for (int t = 0; t < kSub; ++t) {
+                const float m = kP1s ? my_p1[t * 32 * kEpiWarps] : P1[kP1s ? 0 : t];
+                hot1 |= (m >= thr) ? (1u << t) : 0u;
             }
-            const bool cert = (M - R) > E2;  // false for NaN / infinities
+#pragma unroll
+            for (int t = 0; t < 32; ++t) hot2 |= (P2[t] >= thr) ? (1u << t) : 0u;
+            bool loser_hot = fminf(Mh, Mo) >= thr;
+            if (!(thr == thr)) {  // cannot happen with finite operands; recheck all
+                hot1 = kAll1;
+                hot2 = ~0u;
+                loser_hot = true;
+            }
             int code = -1;  // handoff to the update warps: >= 0 label, <= -2 recheck slot
             if (i < n) {
-                if (!cert) {
-                    const float thr = M - E2;
-                    uint32_t hot2 = 0u;
-#pragma unroll
-                    for (int t = 0; t < 32; ++t)
-                        if (P2[t] >= thr) hot2 |= 1u << t;
-                    if (a.keep_p1) {
-                        hot1 = 0u;
-                        for (int sc = 0; sc < nsc_h; ++sc)
-                            if (my_p1[sc * 256] >= thr) hot1 |= 1u << sc;
-                    }
-                    uint32_t *cw = reinterpret_cast<uint32_t *>(a.cand + i);
-                    cw[h] = hot1;
-                    cw[2 + h] = hot2;
-                    if (h == 0) {
+                uint32_t *cw = reinterpret_cast<uint32_t *>(a.cand + i);
+                if (win) {
+                    if (!loser_hot && __popc(hot1) == 1 && __popc(hot2) == 1) {
+                        const int sc = __ffs(hot1) - 1, t = __ffs(hot2) - 1;
+                        code = (sc >> 2) * kChunkN + h * 128 + (sc & 3) * 32 + t;
+                        if (a.label64)
+                            reinterpret_cast<int64_t *>(a.labels)[i] = code;
+                        else
+                            reinterpret_cast<int32_t *>(a.labels)[i] = code;
+                    } else {
+                        cw[h] = hot1;
+                        cw[2 + h] = hot2;
+                        if (!loser_hot) {
+                            cw[h ^ 1] = 0u;
+                            cw[2 + (h ^ 1)] = 0u;
+                        }
                         const int pos = atomicAdd(a.n_flagged, 1);
                         if (pos >= 0 && pos < n) {
                             a.flagged[pos] = (int)i;
                             code = -2 - pos;
                         }
                     }
-                } else {
-                    code = jw;
-                    if (h == 0) {
-                        if (a.label64)
-                            reinterpret_cast<int64_t *>(a.labels)[i] = jw;
-                        else
-                            reinterpret_cast<int32_t *>(a.labels)[i] = jw;
-                    }
+                } else if (loser_hot) {
+                    cw[h] = hot1;
+                    cw[2 + h] = hot2;
                 }
             }
-            if (h == 0) {
-                const int tb = tl & 1;
-                if (mbar_wait(&uempty[tb], (((uint32_t)tl >> 1) & 1u) ^ 1u, err)) {
-                    lab_s[tb * kTileM + row] = code;
-                    mbar_arrive(&ufull[tb]);
-                }
+            const int tb = tl & 1;
+            if (mbar_wait(&uempty[tb], (((uint32_t)tl >> 1) & 1u) ^ 1u, err) && win) {
+                lab_s[tb * kTileM + row] = code;
+                mbar_arrive(&ufull[tb]);
             }
         }
     } else {
         // ------------------------------ update --------------------------------
-        // One thread per tile row.  The row's features are loaded before its
-        // label is known, so the loads overlap the epilogue of the same tile.
-        const int row = threadIdx.x - 32 * (2 + kEpiWarps);
-        const int64_t d = a.d, d4 = a.d4;
+        // Thread u handles rows u and u + 64 of every tile.  The rows (from
+        // the row-major fp32 copy of X) and weights are loaded before their
+        // labels are known, so the loads overlap the epilogue of the tile.
+        // Uncertified rows are left to the recheck kernel.
+        const int u = threadIdx.x - 32 * (2 + kEpiWarps);
+        const int64_t d4 = a.d4;
+        const int64_t cstride = k_pad * d4 + k_pad;
+        float *sums32 = a.sums32 + (int64_t)(blockIdx.x % (unsigned)a.n_copies) * cstride;
+        double *acc64 = a.acc64 + (int64_t)(blockIdx.x % (unsigned)a.n_copies) * cstride;
+        auto consume = [&](int code, const float4 (&xv)[16], float wv, int pass) {
+            if (code < 0 || code >= k || !a.update) return;
+            if (a.acc_f64) {
+                // small d: float64 sums keep the trajectory on the reference's
+                double *dst = acc64 + (int64_t)code * d4 + pass * 64;
+#pragma unroll
+                for (int g = 0; g < 16; ++g) {
+                    if ((int64_t)pass * 64 + 4 * g < d4) {
+                        atomicAdd(dst + 4 * g + 0, (double)__fmul_rn(xv[g].x, wv));
+                        atomicAdd(dst + 4 * g + 1, (double)__fmul_rn(xv[g].y, wv));
+                        atomicAdd(dst + 4 * g + 2, (double)__fmul_rn(xv[g].z, wv));
+                        atomicAdd(dst + 4 * g + 3, (double)__fmul_rn(xv[g].w, wv));
+                    }
+                }
+                if (pass == 0) atomicAdd(acc64 + k_pad * d4 + code, (double)wv);
+            } else {
+                float4 *dst = reinterpret_cast<float4 *>(sums32 + (int64_t)code * d4 + pass * 64);
+#pragma unroll
+                for (int g = 0; g < 16; ++g) {
+                    if ((int64_t)pass * 64 + 4 * g < d4) {
+                        float4 v;
+                        v.x = __fmul_rn(xv[g].x, wv);
+                        v.y = __fmul_rn(xv[g].y, wv);
+                        v.z = __fmul_rn(xv[g].z, wv);
+                        v.w = __fmul_rn(xv[g].w, wv);
+                        atomicAdd(dst + g, v);
+                    }
+                }
+                if (pass == 0) atomicAdd(sums32 + k_pad * d4 + code, wv);
+            }
+        };
         int tl = 0;
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tl) {
             const int tb = tl & 1;
-            const int64_t i = tile * kTileM + row;
-            int code = -1;
+            const int64_t i0 = tile * kTileM + u, i1 = i0 + 64;
+            const float w0 = (a.update && i0 < n) ? __ldg(a.w + i0) : 0.f;
+            const float w1 = (a.update && i1 < n) ? __ldg(a.w + i1) : 0.f;
+            int c0 = -1, c1 = -1;
             bool have_code = false;
-            float wv = 0.f;
 #pragma unroll 1
             for (int pass = 0; pass < NKB; ++pass) {
-                float xv[64];
+                float4 xa[16], xb[16];
+                const float4 *ra = reinterpret_cast<const float4 *>(a.xrow + i0 * d4 + pass * 64);
+                const float4 *rb = reinterpret_cast<const float4 *>(a.xrow + i1 * d4 + pass * 64);
 #pragma unroll
-                for (int f = 0; f < 64; ++f) {
-                    const int64_t F = (int64_t)pass * 64 + f;
-                    xv[f] = (i < n && F < d) ? __ldg(a.X + F * n + i) : 0.f;
+                for (int g = 0; g < 16; ++g) {
+                    const bool in = (int64_t)pass * 64 + 4 * g < d4;
+                    xa[g] = (a.update && in && i0 < n) ? __ldg(ra + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    xb[g] = (a.update && in && i1 < n) ? __ldg(rb + g) : make_float4(0.f, 0.f, 0.f, 0.f);
                 }
                 if (!have_code) {
                     if (!mbar_wait(&ufull[tb], ((uint32_t)tl >> 1) & 1u, err)) break;
-                    code = lab_s[tb * kTileM + row];
+                    c0 = lab_s[tb * kTileM + u];
+                    c1 = lab_s[tb * kTileM + u + 64];
                     mbar_arrive(&uempty[tb]);
                     have_code = true;
-                    if (code >= 0 && a.update) wv = a.w[i];
                 }
-                if (code >= 0 && code < k && a.update) {
-                    if (a.priv64) {
-                        double *ps = priv + (int64_t)code * d4 + pass * 64;
-#pragma unroll
-                        for (int f = 0; f < 64; ++f)
-                            if ((int64_t)pass * 64 + f < d) atomicAdd(ps + f, (double)__fmul_rn(xv[f], wv));
-                        if (pass == 0) atomicAdd(priv + k_pad * d4 + code, (double)wv);
-                    } else {
-                        float4 *dst = reinterpret_cast<float4 *>(a.sums32 + (int64_t)code * d4 + pass * 64);
-#pragma unroll
-                        for (int g = 0; g < 16; ++g) {
-                            if ((int64_t)pass * 64 + 4 * g < d4) {
-                                float4 v;
-                                v.x = __fmul_rn(xv[4 * g + 0], wv);
-                                v.y = __fmul_rn(xv[4 * g + 1], wv);
-                                v.z = __fmul_rn(xv[4 * g + 2], wv);
-                                v.w = __fmul_rn(xv[4 * g + 3], wv);
-                                atomicAdd(dst + g, v);
-                            }
-                        }
-                        if (pass == 0) atomicAdd(a.sizes32 + code, wv);
-                    }
-                } else if (code <= -2) {
-                    // stage the row for the exact recheck (contiguous, fp32)
-                    const int64_t pos = -2 - (int64_t)code;
-                    float4 *dst = reinterpret_cast<float4 *>(a.xflag + pos * d4 + pass * 64);
-#pragma unroll
-                    for (int g = 0; g < 16; ++g)
-                        if ((int64_t)pass * 64 + 4 * g < d4)
-                            dst[g] = make_float4(xv[4 * g], xv[4 * g + 1], xv[4 * g + 2], xv[4 * g + 3]);
-                }
+                consume(c0, xa, w0, pass);
+                consume(c1, xb, w1, pass);
             }
             if (!have_code) break;
-        }
-        if (a.priv64) {
-            // all update threads are done with the shared sums: flush them
-            asm volatile("bar.sync 2, 128;" ::: "memory");
-            for (int64_t e = row; e < k_pad * d4 + k_pad; e += kTileM) {
-                const double v = priv[e];
-                if (v != 0.0) atomicAdd(a.acc64 + e, v);
-            }
         }
     }
 
@@ -646,6 +641,7 @@ __global__ void absmax_kernel(const float *X, int64_t count, unsigned int *out_b
 // shares fp32's exponent range and is never scaled.
 __global__ void sigma_kernel(MixedConsts *c, int bf16, int64_t d) {
     const double xmax = (double)__uint_as_float(c->xmax_bits);
+
     double sigma = 1.0;
     if (!bf16 && xmax > 0.0 && xmax < 1e300) {
         const double hx = 0.5 * (double)d * xmax * xmax;
@@ -659,11 +655,13 @@ __global__ void sigma_kernel(MixedConsts *c, int bf16, int64_t d) {
 }
 
 // One thread per sample row (including the zero rows that pad the last
-// tile): the 128-byte-swizzled K-major image of (x * sigma), and the norms
-// ||x||_2, ||x||_1 rounded up.
+// tile): the 128-byte-swizzled K-major image of (x * sigma), the row-major
+// fp32 copy of x (features d..d4-1 zero), and the norms ||x||_2, ||x||_1
+// rounded up.
 template <int BF16>
-__global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int nkb, int64_t rows,
-                               const MixedConsts *c, uint8_t *img, float *nx, float *n1) {
+__global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int64_t d4, int nkb,
+                               int64_t rows, const MixedConsts *c, uint8_t *img, float *xrow,
+                               float *nx, float *n1) {
     const float sigma = c->sigma;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -673,7 +671,7 @@ __global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int nkb, in
         for (int kb = 0; kb < nkb; ++kb) {
             uint8_t *base = img + ((size_t)tile * nkb + kb) * kTileBytes;
             for (int ch = 0; ch < 8; ++ch) {
-                float v[8];
+                float v[8], xr[8];
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
                     const int64_t f = (int64_t)kb * 64 + ch * 8 + e;
@@ -681,6 +679,13 @@ __global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int nkb, in
                     s2 += (double)x * (double)x;
                     s1 += fabs((double)x);
                     v[e] = x * sigma;
+                    xr[e] = x;
+                }
+                if (i < n) {
+                    const int64_t f0 = (int64_t)kb * 64 + ch * 8;
+                    float4 *dst = reinterpret_cast<float4 *>(xrow + i * d4 + f0);
+                    if (f0 < d4) dst[0] = make_float4(xr[0], xr[1], xr[2], xr[3]);
+                    if (f0 + 4 < d4) dst[1] = make_float4(xr[4], xr[5], xr[6], xr[7]);
                 }
                 uint4 pk;
                 pk.x = pack2<BF16>(v[0], v[1]);
@@ -838,17 +843,23 @@ __global__ void bound_kernel(const float *cn2, const float *cn1, const float *hn
 // Exact fp32 re-evaluation of samples whose margin did not certify them: the
 // reference's arithmetic (sequential fma dot, hn - dot, strict < in
 // ascending centroid order) over the candidate set, one warp per sample.  The
-// sample's features come from the compact rows staged by the update warps and
-// the centroids from their transposed fp32 copy (one contiguous row each).
-__global__ void recheck_kernel(const float *xflag, const float *ct, const float *hn,
+// sample's features come from the row-major fp32 copy of X and the centroids
+// from their transposed fp32 copy (one contiguous row each).
+__global__ void recheck_kernel(const float *xrow, const float *ct, const float *hn,
                                const float *w, const uint4 *cand, const int *flagged,
                                const int *n_flagged, int64_t n, int64_t d, int64_t k, int64_t d4,
-                               void *labels, int label64, int update, int priv64, float *sums32,
-                               float *sizes32, double *acc64, int64_t k_pad,
+                               void *labels, int label64, int update, int acc_f64, float *sums32,
+                               double *acc64, int64_t k_pad, int n_copies,
                                const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
     extern __shared__ __align__(16) float xs[];  // [warps][d4]
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    {
+        // this block's share of the per-CTA copies of the cluster sums
+        const int64_t copy = (int64_t)(blockIdx.x % (unsigned)n_copies) * (k_pad * d4 + k_pad);
+        sums32 += copy;
+        acc64 += copy;
+    }
     float *x = xs + (size_t)wib * d4;
     const int64_t nf = (int64_t)*n_flagged;
     const int64_t total = nf < n ? nf : n;
@@ -856,7 +867,7 @@ __global__ void recheck_kernel(const float *xflag, const float *ct, const float 
     for (int64_t e = blockIdx.x * (int64_t)(blockDim.x >> 5) + wib; e < total; e += nwarps) {
         const int64_t i = flagged[e];
         if (i < 0 || i >= n) continue;
-        for (int64_t f = lane; f < d4; f += 32) x[f] = xflag[e * d4 + f];
+        for (int64_t f = lane; f < d4; f += 32) x[f] = xrow[i * d4 + f];
         __syncwarp();
         const uint4 cm = cand[i];
         const uint32_t h1[2] = {cm.x, cm.y}, h2[2] = {cm.z, cm.w};
@@ -912,52 +923,55 @@ __global__ void recheck_kernel(const float *xflag, const float *ct, const float 
             const float wv = w[i];
             for (int64_t f = lane; f < d; f += 32) {
                 const float v = __fmul_rn(x[f], wv);
-                if (priv64)
+                if (acc_f64)
                     atomicAdd(acc64 + (int64_t)bj * d4 + f, (double)v);
                 else
                     atomicAdd(sums32 + (int64_t)bj * d4 + f, v);
             }
             if (lane == 0) {
-                if (priv64)
+                if (acc_f64)
                     atomicAdd(acc64 + k_pad * d4 + bj, (double)wv);
                 else
-                    atomicAdd(sizes32 + bj, wv);
+                    atomicAdd(sums32 + k_pad * d4 + bj, wv);
             }
         }
         __syncwarp();
     }
 }
 
-// Cluster-major sums (fp32 or fp64) -> (d, k) centroid sums and sizes in
-// dataT, rounded once.
+// Per-CTA copies of the cluster-major sums (fp32 or fp64) -> (d, k) centroid
+// sums and sizes in dataT: copies added in index order in fp64, rounded once.
 template <typename A>
-__global__ void km_to_dk_kernel(const A *sums_km, const A *sizes_acc, float *out_c,
-                                float *out_sizes, int64_t d, int64_t k, int64_t d4,
+__global__ void km_to_dk_kernel(const A *copies, int n_copies, float *out_c, float *out_sizes,
+                                int64_t d, int64_t k, int64_t k_pad, int64_t d4,
                                 const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < d * k + k;
+    const int64_t cs = k_pad * d4 + k_pad;
+    // consecutive threads read consecutive words of every copy
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * d4 + k;
          e += (int64_t)gridDim.x * blockDim.x) {
-        if (e < d * k) {
-            const int64_t f = e / k, j = e % k;
-            out_c[e] = (float)sums_km[j * d4 + f];
-        } else {
-            out_sizes[e - d * k] = (float)sizes_acc[e - d * k];
-        }
+        const bool is_size = e >= k * d4;
+        const int64_t off = is_size ? k_pad * d4 + (e - k * d4) : e;
+        const int64_t j = e / d4, f = e % d4;
+        if (!is_size && f >= d) continue;
+        double acc = 0.0;
+        for (int c = 0; c < n_copies; ++c) acc += (double)copies[(int64_t)c * cs + off];
+        if (is_size)
+            out_sizes[e - k * d4] = (float)acc;
+        else
+            out_c[f * k + j] = (float)acc;
     }
 }
 
-__global__ void reset_kernel(float *sums32, float *sizes32, double *acc64, int64_t count,
-                             int64_t k_pad, int priv64, int *n_flagged, const LoopState *guard) {
+__global__ void reset_kernel(float *sums32, double *acc64, int64_t count, int acc_f64,
+                             int *n_flagged, const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count + k_pad;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count;
          e += (int64_t)gridDim.x * blockDim.x) {
-        if (priv64) {
+        if (acc_f64)
             acc64[e] = 0.0;
-        } else if (e < count) {
+        else
             sums32[e] = 0.f;
-        } else {
-            sizes32[e - count] = 0.f;
-        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *n_flagged = 0;
 }
@@ -968,6 +982,27 @@ __global__ void stats_kernel(const int *n_flagged, long long *last, long long *t
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
     *last = *n_flagged;
     *total += *n_flagged;
+}
+
+using MixedKernel = void (*)(MixedArgs);
+
+template <int BF16, int NKB>
+MixedKernel pick_chunks(int nch) {
+    switch (nch) {
+        case 1: return mixed_assign_kernel<BF16, NKB, 1>;
+        case 2: return mixed_assign_kernel<BF16, NKB, 2>;
+        case 3: return NKB == 1 ? mixed_assign_kernel<BF16, 1, 3> : nullptr;
+        case 4: return NKB == 1 ? mixed_assign_kernel<BF16, 1, 4> : nullptr;
+        default: return nullptr;
+    }
+}
+
+// Kernel for (operand type, 64-feature blocks, 256-column chunks).  Two
+// feature blocks leave shared memory for at most two chunks.
+MixedKernel pick_kernel(int bf16, int nkb, int nch) {
+    if (nkb == 1) return bf16 ? pick_chunks<1, 1>(nch) : pick_chunks<0, 1>(nch);
+    if (nkb == 2) return bf16 ? pick_chunks<1, 2>(nch) : pick_chunks<0, 2>(nch);
+    return nullptr;
 }
 
 unsigned grid1d(int64_t work, int block, int cap = 8192) {
@@ -983,15 +1018,15 @@ struct MixedFit : PlainFit<float, I> {
     using Base = PlainFit<float, I>;
     int bf16 = 0;
     int nkb = 1;
-    int priv64 = 0;
-    int keep_p1 = 0;
+    int acc_f64 = 0;
     int stages = 2;
     int64_t k_pad = 0, d4 = 0, ntiles = 0;
     Scratch mws;
     uint8_t *ximg = nullptr, *cimg = nullptr;
-    float *nx = nullptr, *n1 = nullptr, *ct = nullptr, *xflag = nullptr;
-    float *sums32 = nullptr, *sizes32 = nullptr;
+    float *nx = nullptr, *n1 = nullptr, *ct = nullptr, *xrow = nullptr;
+    float *sums32 = nullptr;
     double *acc64 = nullptr;
+    int n_copies = 1;  // private copies of the cluster sums (one per CTA)
     float *cn2 = nullptr, *cn1 = nullptr;
     MixedConsts *consts = nullptr;
     uint4 *cand = nullptr;
@@ -1001,9 +1036,9 @@ struct MixedFit : PlainFit<float, I> {
     static bool supported(int64_t d, int64_t k) {
         const int nk = (int)ceil_div<int64_t>(std::max<int64_t>(d, 1), 64);
         const int64_t kp = ceil_div<int64_t>(std::max<int64_t>(k, 1), kChunkN) * kChunkN;
-        if (nk > 2 || kp > kMaxKPad) return false;
+        if (nk > 2 || kp > (int64_t)kMaxChunks * kChunkN) return false;
         const int64_t dd = ceil_div<int64_t>(std::max<int64_t>(d, 1), 4) * 4;
-        return smem_layout(nk, kp, dd, 0, 0, 2).total <= kSmemLimit;
+        return smem_layout(nk, kp, dd, 2).total <= kSmemLimit;
     }
 
     int init_mixed(int form) {
@@ -1014,20 +1049,17 @@ struct MixedFit : PlainFit<float, I> {
         k_pad = ceil_div<int64_t>(p.k, kChunkN) * kChunkN;
         d4 = ceil_div<int64_t>(std::max<int64_t>(p.d, 1), 4) * 4;
         ntiles = ceil_div<int64_t>(p.n, kTileM);
-        // shared memory, in order of preference: float64 cluster sums (they
-        // keep the trajectory close to the float64 reference), then the
-        // deepest X ring, then the exact sub-chunk maxima
-        static const int kChoices[6][2] = {{4, 1}, {3, 1}, {4, 0}, {3, 0}, {2, 1}, {2, 0}};
+        // Cluster sums: up to 32 features, float64 reductions per feature
+        // (a few per sample; they keep the trajectory on the float64
+        // reference's), beyond that float32 four-wide reductions.
+        acc_f64 = d4 <= 32 ? 1 : 0;
+        // the deepest X ring that fits next to the centroid image
         bool found = false;
-        for (int pv = 1; pv >= 0 && !found; --pv)
-            for (int q = 0; q < 6 && !found; ++q)
-                if (smem_layout(nkb, k_pad, d4, pv, kChoices[q][1], kChoices[q][0]).total <=
-                    kSmemLimit) {
-                    priv64 = pv;
-                    stages = kChoices[q][0];
-                    keep_p1 = kChoices[q][1];
-                    found = true;
-                }
+        for (int st = 4; st >= 2 && !found; --st)
+            if (smem_layout(nkb, k_pad, d4, st).total <= kSmemLimit) {
+                stages = st;
+                found = true;
+            }
         if (!found) {
             set_error("mixed form: operands do not fit in shared memory");
             return KMC_ERR_UNSUPPORTED;
@@ -1043,8 +1075,16 @@ struct MixedFit : PlainFit<float, I> {
         const size_t o_ct = take(sizeof(float) * k_pad * d4);
         const size_t o_nx = take(sizeof(float) * p.n);
         const size_t o_n1 = take(sizeof(float) * p.n);
-        const size_t o_s32 = take(priv64 ? 16 : sizeof(float) * (k_pad * d4 + k_pad));
-        const size_t o_a64 = take(priv64 ? sizeof(double) * (k_pad * d4 + k_pad) : 16);
+        // Small sums get one private copy per CTA of the assignment: their
+        // few addresses would otherwise serialise the reductions of all SMs.
+        // Large ones (c3-sized, 266 KB) stay single: per-CTA copies would
+        // crowd L2 for less contention than they remove.
+        n_copies = (k_pad * d4 <= 32768)
+                       ? (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, num_sms()))
+                       : 1;
+        const int64_t csz = (int64_t)n_copies * (k_pad * d4 + k_pad);
+        const size_t o_s32 = take(acc_f64 ? 16 : sizeof(float) * csz);
+        const size_t o_a64 = take(acc_f64 ? sizeof(double) * csz : 16);
         const size_t o_xf = take(sizeof(float) * std::max<int64_t>(p.n, 1) * d4);
         const size_t o_cn2 = take(sizeof(float) * p.k);
         const size_t o_cn1 = take(sizeof(float) * p.k);
@@ -1061,9 +1101,8 @@ struct MixedFit : PlainFit<float, I> {
         nx = reinterpret_cast<float *>(b + o_nx);
         n1 = reinterpret_cast<float *>(b + o_n1);
         sums32 = reinterpret_cast<float *>(b + o_s32);
-        sizes32 = sums32 + k_pad * d4;
         acc64 = reinterpret_cast<double *>(b + o_a64);
-        xflag = reinterpret_cast<float *>(b + o_xf);
+        xrow = reinterpret_cast<float *>(b + o_xf);
         cn2 = reinterpret_cast<float *>(b + o_cn2);
         cn1 = reinterpret_cast<float *>(b + o_cn1);
         consts = reinterpret_cast<MixedConsts *>(b + o_cst);
@@ -1083,11 +1122,11 @@ struct MixedFit : PlainFit<float, I> {
         KMC_TRY(check_launch("sigma"));
         const int64_t rows = ntiles * kTileM;
         if (bf16)
-            x_image_kernel<1><<<grid1d(rows, 256, 1 << 20), 256, 0, s>>>(p.X, p.n, p.d, nkb, rows,
-                                                                        consts, ximg, nx, n1);
+            x_image_kernel<1><<<grid1d(rows, 256, 1 << 20), 256, 0, s>>>(
+                p.X, p.n, p.d, d4, nkb, rows, consts, ximg, xrow, nx, n1);
         else
-            x_image_kernel<0><<<grid1d(rows, 256, 1 << 20), 256, 0, s>>>(p.X, p.n, p.d, nkb, rows,
-                                                                        consts, ximg, nx, n1);
+            x_image_kernel<0><<<grid1d(rows, 256, 1 << 20), 256, 0, s>>>(
+                p.X, p.n, p.d, d4, nkb, rows, consts, ximg, xrow, nx, n1);
         KMC_TRY(check_launch("x_image"));
         this->launches += 3;
         return KMC_OK;
@@ -1111,8 +1150,9 @@ struct MixedFit : PlainFit<float, I> {
         const FitParams<float, I> &p = this->prm;
         cudaStream_t s = p.stream;
         KMC_TRY(centroid_prep(cur, guard));
-        reset_kernel<<<grid1d(k_pad * d4 + k_pad, 256, 2048), 256, 0, s>>>(
-            sums32, sizes32, acc64, k_pad * d4, k_pad, priv64, n_flagged, guard);
+        const int64_t csz = (int64_t)n_copies * (k_pad * d4 + k_pad);
+        reset_kernel<<<grid1d(csz, 256, 4096), 256, 0, s>>>(sums32, acc64, csz, acc_f64,
+                                                           n_flagged, guard);
         KMC_TRY(check_launch("mixed_reset"));
         MixedArgs a;
         a.ximg = ximg;
@@ -1124,9 +1164,9 @@ struct MixedFit : PlainFit<float, I> {
         a.w = p.w;
         a.labels = p.labels;
         a.sums32 = sums32;
-        a.sizes32 = sizes32;
         a.acc64 = acc64;
-        a.xflag = xflag;
+        a.n_copies = n_copies;
+        a.xrow = xrow;
         a.cand = cand;
         a.flagged = flagged;
         a.n_flagged = n_flagged;
@@ -1139,12 +1179,15 @@ struct MixedFit : PlainFit<float, I> {
         a.d4 = d4;
         a.update = update;
         a.label64 = sizeof(I) == 8 ? 1 : 0;
-        a.priv64 = priv64;
-        a.keep_p1 = keep_p1;
+        a.acc_f64 = acc_f64;
         a.stages = stages;
-        const SmemLayout L = smem_layout(nkb, k_pad, d4, priv64, keep_p1, stages);
-        auto kern = bf16 ? (nkb == 1 ? mixed_assign_kernel<1, 1> : mixed_assign_kernel<1, 2>)
-                         : (nkb == 1 ? mixed_assign_kernel<0, 1> : mixed_assign_kernel<0, 2>);
+        const SmemLayout L = smem_layout(nkb, k_pad, d4, stages);
+        auto kern = pick_kernel(bf16, nkb, (int)(k_pad / kChunkN));
+        if (kern == nullptr) {
+            set_error("mixed form: no kernel for %d feature blocks and %lld chunks", nkb,
+                      (long long)(k_pad / kChunkN));
+            return KMC_ERR_UNSUPPORTED;
+        }
         KMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)L.total));
         const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(ntiles, num_sms()));
@@ -1155,8 +1198,8 @@ struct MixedFit : PlainFit<float, I> {
         const int rblock = 256;
         const size_t rsmem = sizeof(float) * (rblock / 32) * d4;
         recheck_kernel<<<(unsigned)(num_sms() * 4), rblock, rsmem, s>>>(
-            xflag, ct, this->hn, p.w, cand, flagged, n_flagged, p.n, p.d, p.k, d4, p.labels,
-            a.label64, update, priv64, sums32, sizes32, acc64, k_pad, guard);
+            xrow, ct, this->hn, p.w, cand, flagged, n_flagged, p.n, p.d, p.k, d4, p.labels,
+            a.label64, update, acc_f64, sums32, acc64, k_pad, n_copies, guard);
         KMC_TRY(check_launch("mixed_recheck"));
         stats_kernel<<<1, 1, 0, s>>>(n_flagged, stats, stats + 1, guard);
         return check_launch("mixed_stats");
@@ -1170,12 +1213,12 @@ struct MixedFit : PlainFit<float, I> {
     int reduce_step(float *nxt) override {
         const FitParams<float, I> &p = this->prm;
         cudaStream_t s = p.stream;
-        if (priv64)
-            km_to_dk_kernel<double><<<grid1d(p.d * p.k + p.k, 256, 4096), 256, 0, s>>>(
-                acc64, acc64 + k_pad * d4, nxt, this->sizes, p.d, p.k, d4, this->state);
+        if (acc_f64)
+            km_to_dk_kernel<double><<<grid1d(p.k * d4 + p.k, 256, 4096), 256, 0, s>>>(
+                acc64, n_copies, nxt, this->sizes, p.d, p.k, k_pad, d4, this->state);
         else
-            km_to_dk_kernel<float><<<grid1d(p.d * p.k + p.k, 256, 4096), 256, 0, s>>>(
-                sums32, sizes32, nxt, this->sizes, p.d, p.k, d4, this->state);
+            km_to_dk_kernel<float><<<grid1d(p.k * d4 + p.k, 256, 4096), 256, 0, s>>>(
+                sums32, n_copies, nxt, this->sizes, p.d, p.k, k_pad, d4, this->state);
         KMC_TRY(check_launch("km_to_dk"));
         return launch_empty_list<float, I>(this->sizes, this->empty_list, this->n_empty, p.k, s,
                                            this->state);
@@ -1207,7 +1250,7 @@ int make_mixed_fit(const FitParams<T, I> &p, int form, std::unique_ptr<FitBase> 
         if (!MixedFit<I>::supported(p.d, p.k)) {
             set_error("mixed form supports n_features <= 128 and n_clusters <= %d within %zu "
                       "bytes of shared memory (got d=%lld, k=%lld)",
-                      kMaxKPad, kSmemLimit, (long long)p.d, (long long)p.k);
+                      kMaxChunks * kChunkN, kSmemLimit, (long long)p.d, (long long)p.k);
             return KMC_ERR_UNSUPPORTED;
         }
         auto f = std::make_unique<MixedFit<I>>();

@@ -2,10 +2,9 @@
 
 Labels from one mixed assignment pass must equal the exact reference labels
 for every sample: samples whose tensor-core margin does not certify them are
-re-evaluated in exact float32.  Full fits accumulate centroid sums in float32
-atomics, so their trajectories are compared with tolerances: labels identical
-except for samples whose top-two relative gap is below 1e-5, centroids and
-inertia within 1e-5 relative.
+re-evaluated in exact float32.  Full fits are compared with tolerances: labels
+identical except for samples whose top-two relative gap is below 1e-5,
+centroids and inertia within 1e-5 relative.
 """
 import ctypes
 
@@ -95,10 +94,10 @@ def _near_tie_mask(X, C, rel=1e-5):
     return (part[:, 1] - part[:, 0]) <= rel * np.maximum(part[:, 1], 1e-30)
 
 
+# Up to 32 features the cluster sums are reduced in float64, so whole
+# trajectories follow the oracle's (iteration count included).
 @pytest.mark.parametrize("case", [("c1_50k_d14_k16", 50_000, 14, 16, 16, (-10, 10), 1.0, 0, 1e-4, 100),
-                                  ("d64_k256", 60_000, 64, 256, 256, (-5, 5), 1.0, 2, 0.0, 8),
-                                  ("d64_k1024_sigma", 100_000, 64, 1024, 1024, (-5, 5), (0.5, 2.0), 2,
-                                   0.0, 5)])
+                                  ("d32_k200", 40_000, 32, 100, 200, (-5, 5), 1.0, 3, 0.0, 10)])
 @pytest.mark.parametrize("form", sorted(FORMS))
 def test_mixed_driver_tracks_oracle(oracle, case, form):
     name, n, d, centers, k, box, std, seed, tol, max_iter = case
@@ -111,3 +110,54 @@ def test_mixed_driver_tracks_oracle(oracle, case, form):
     assert not np.any(diff & ~_near_tie_mask(X, C_o)), int(diff.sum())
     np.testing.assert_allclose(C_g, C_o, rtol=1e-5, atol=1e-5 * np.abs(C_o).max())
     assert inr_g == pytest.approx(inr_o, rel=1e-5)
+
+
+# Beyond 32 features the sums are float32 reductions in arrival order (as the
+# reference's atomics are), so trajectories are compared one iteration at a
+# time: labels exact against the oracle at that iteration's centroids, the
+# update within float32 accumulation tolerance, and the final pass exact.
+@pytest.mark.parametrize("case", [("d64_k256", 60_000, 64, 256, 256, (-5, 5), 1.0, 2, 6),
+                                  ("d64_k1024_sigma", 100_000, 64, 1024, 1024, (-5, 5), (0.5, 2.0), 2, 4),
+                                  ("d100_k300", 30_000, 100, 150, 300, (-5, 5), 1.0, 4, 3)])
+@pytest.mark.parametrize("form", sorted(FORMS))
+def test_mixed_iterations_match_oracle_step_by_step(oracle, case, form):
+    import torch
+
+    from kmeans_dpcpp_gb300 import capi
+
+    name, n, d, centers, k, box, std, seed, iters = case
+    X, _, _ = bench.make_blobs(n, d, centers, box, std, seed)
+    C0 = bench.random_row_init(X, k, seed)
+    w = np.ones(n, np.float32)
+    L = capi.lib()
+    Xg = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+    wg = torch.from_numpy(w).cuda()
+    cur = torch.from_numpy(np.ascontiguousarray(C0).copy()).cuda()
+    res = torch.empty_like(cur)
+    lab = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    fit = ctypes.c_void_p()
+    capi.check(L.kmc_fit_create_f32_i32(Xg.data_ptr(), wg.data_ptr(), cur.data_ptr(), lab.data_ptr(),
+                                        res.data_ptr(), n, d, k, 0.0, iters, FORMS[form],
+                                        stream.cuda_stream, ctypes.byref(fit)))
+    try:
+        for _ in range(iters):
+            C_before = cur.cpu().numpy().copy()
+            capi.check(L.kmc_fit_step(fit, 1))
+            stream.synchronize()
+            np.testing.assert_array_equal(lab.cpu().numpy(), oracle.assignment(X, C_before))
+            _, _, C_o, _, _ = oracle.kmeans_lloyd_driver(X, w, C_before, 0.0, 1)
+            C_after = cur.cpu().numpy()
+            np.testing.assert_allclose(C_after, C_o, rtol=1e-5, atol=1e-5 * np.abs(C_o).max())
+        it, inertia = ctypes.c_int64(), ctypes.c_double()
+        capi.check(L.kmc_fit_finalize(fit, ctypes.byref(it), ctypes.byref(inertia)))
+        last, total, err = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
+        capi.check(L.kmc_fit_rechecked(fit, ctypes.byref(last), ctypes.byref(total), ctypes.byref(err)))
+    finally:
+        capi.check(L.kmc_fit_destroy(fit))
+    assert err.value == 0 and it.value == iters
+    C_final = res.cpu().numpy()
+    lab_final = lab.cpu().numpy()
+    np.testing.assert_array_equal(lab_final, oracle.assignment(X, C_final))
+    inr_o = float(np.sum(oracle.compute_inertia(X, w, C_final, lab_final).astype(np.float64)))
+    assert inertia.value == pytest.approx(inr_o, rel=1e-6)
