@@ -60,6 +60,13 @@ WORKLOADS = {
 
 FORMS = {"plain": 0, "mixed-bf16": 1, "mixed-fp16": 2}
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the dominant kernel per sample, from one ncu capture at n=1,000,000 of the
+# workload's shape (profiles/mixed_assign_c3_n1M.txt and
+# profiles/tile_kernel_plain_c3_n1M.txt); the kernels stream every sample
+# once, so a launch's traffic scales with n.
+TRAFFIC_PER_SAMPLE = {("c3", "mixed-fp16"): 405.8, ("c3", "plain"): 267.6}
+
 
 # ---------------------------------------------------------------------------
 # synthetic data (shared with the tests)
@@ -99,8 +106,17 @@ def random_row_init(X_t, k, seed, far_first=False):
     return C
 
 
-def workload_data(name):
-    w = WORKLOADS[name]
+def workload(name, n=None):
+    """The named workload, optionally with fewer samples (profiling captures)."""
+    w = dict(WORKLOADS[name])
+    if n:
+        w["n"] = int(n)
+        w["desc"] = w["desc"] + " (n reduced to %d)" % w["n"]
+    return w
+
+
+def workload_data(name, n=None):
+    w = workload(name, n)
     X_t, _, _ = make_blobs(w["n"], w["d"], w["centers"], w["box"], w["std"], w["seed"])
     C0 = random_row_init(X_t, w["k"], w["seed"], far_first=w["far_first"])
     return X_t, C0
@@ -248,8 +264,8 @@ def run_reference(args, world, rank):
 
     if rank != 0:
         return
-    w = WORKLOADS[args.workload]
-    X_t, C0 = workload_data(args.workload)
+    w = workload(args.workload, args.n)
+    X_t, C0 = workload_data(args.workload, args.n)
     n = X_t.shape[1]
     n_s = calibrate_cpu_sample(X_t, C0, target_s=1.5)
     for _ in range(args.warmup):
@@ -338,7 +354,7 @@ def _time_form(L, capi, Xg, wg, C0, n, d, k, form, steps, warmup, world, local, 
             "clocks": clk.summary() if sample_clocks else None}
 
 
-def _roofline(form, n, d, k, kern_ms, clocks, sm_count):
+def _roofline(workload, form, n, d, k, kern_ms, clocks, sm_count):
     peaks, peak_src = measured_peaks()
     flops = 2.0 * n * k * d
     achieved = flops / (kern_ms * 1e-3) / 1e12
@@ -355,9 +371,15 @@ def _roofline(form, n, d, k, kern_ms, clocks, sm_count):
              "peak_source": f"bf16_tflops_sustained of MEASURED_PEAKS.json ({peak_src}); the "
                             "fp16 dense tensor rate equals the bf16 one",
              "kernel": "mixed_assign_kernel + recheck_kernel (tcgen05 assignment + accumulation)"}
-    r.update({"frac": achieved / peak, "traffic": None, "kernel_ms": kern_ms,
+    per_sample = TRAFFIC_PER_SAMPLE.get((workload, form))
+    r.update({"frac": achieved / peak, "traffic": per_sample * n if per_sample else None,
+              "traffic_source": ("ncu capture at n=1M of this shape, scaled by n" if per_sample
+                                 else "not captured for this workload"),
+              "kernel_ms": kern_ms,
               "flops_per_launch": flops,
-              "algorithmic_bytes_per_launch": n * d * (4 if form == "plain" else 2) + 4 * n})
+              # plain: X (fp32) once + labels; mixed: the fp16/bf16 image for the
+              # contraction, the fp32 rows for the exact sums, labels
+              "algorithmic_bytes_per_launch": n * d * (4 if form == "plain" else 6) + 4 * n})
     return r
 
 
@@ -369,9 +391,9 @@ def run_gb300(args, world, rank, local):
 
     torch.cuda.set_device(local)
     L = capi.lib()
-    w = WORKLOADS[args.workload]
+    w = workload(args.workload, args.n)
     n, d, k = w["n"], w["d"], w["k"]
-    X_t, C0 = workload_data(args.workload)
+    X_t, C0 = workload_data(args.workload, args.n)
     form = "mixed-fp16" if args.form == "auto" else args.form
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
 
@@ -385,7 +407,7 @@ def run_gb300(args, world, rank, local):
                 st = min(args.steps, 10) if other == "plain" else args.steps
                 forms[other] = _time_form(L, capi, Xg, wg, C0, n, d, k, other, st, args.warmup, world,
                                           local, False)
-    roofline = _roofline(form, n, d, k, head["kernel_ms"], head["clocks"], sm_count)
+    roofline = _roofline(args.workload, form, n, d, k, head["kernel_ms"], head["clocks"], sm_count)
 
     # ---- end to end through the drop-in surface, host buffers ----
     e2e = None
@@ -459,6 +481,8 @@ def main(argv=None):
     ap.add_argument("--no-compare", action="store_true",
                     help="time only the headline form (no plain / other mixed comparison)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--n", type=int, default=None,
+                    help="fewer samples than the workload names (small profiling captures)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
