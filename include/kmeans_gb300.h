@@ -442,6 +442,84 @@ int kmc_fit_rechecked(kmc_fit_t fit, int64_t *last_out, int64_t *total_out, int 
 int kmc_fit_launch_count(kmc_fit_t fit, int64_t *launches_out);
 int kmc_fit_destroy(kmc_fit_t fit);
 
+/* ---- batched fits ------------------------------------------------------------------
+ * No counterpart in the reference (the benchmark spec's batching and serving
+ * row).  Many independent float32 fits and label-only predictions of uneven
+ * (n, d, k) advance together, one Lloyd iteration per kmc_batch_step, through
+ * per-phase kernels fed by a device work queue and replayed as CUDA graphs.
+ * Each fit follows kmeans_lloyd_driver's semantics (stop rule, empty-cluster
+ * relocation, final assignment and inertia) with the plain form's arithmetic:
+ * labels equal a single plain fit's, centroids and inertia agree to float64
+ * summation order.  The caller owns X_t, sample_weight, centroids_t (initial
+ * centroids in, final centroids out) and labels until the instance is
+ * removed.  d <= 1024, k <= 4096. */
+typedef struct kmc_batch_s *kmc_batch_t;
+int kmc_batch_create(int64_t max_instances, kmc_stream_t stream, kmc_batch_t *batch_out);
+int kmc_batch_add_fit_f32(kmc_batch_t batch, const float *X_t, const float *sample_weight,
+                          float *centroids_t, int32_t *labels, int64_t n_samples,
+                          int64_t n_features, int64_t n_clusters, double tol, int64_t max_iter,
+                          int64_t *instance_out);
+int kmc_batch_add_predict_f32(kmc_batch_t batch, const float *X_t, const float *centroids_t,
+                              int32_t *labels, int64_t n_samples, int64_t n_features,
+                              int64_t n_clusters, int64_t *instance_out);
+/* One engine step; *n_active_out = instances still running afterwards. */
+int kmc_batch_step(kmc_batch_t batch, int64_t *n_active_out);
+/* Steps until every instance has finished. */
+int kmc_batch_run(kmc_batch_t batch);
+int kmc_batch_result(kmc_batch_t batch, int64_t instance, int *finished_out,
+                     int64_t *n_iter_out, double *inertia_out);
+int kmc_batch_remove(kmc_batch_t batch, int64_t instance);
+int kmc_batch_stats(kmc_batch_t batch, int64_t *steps_out, int64_t *graph_builds_out,
+                    int64_t *relocations_out);
+int kmc_batch_destroy(kmc_batch_t batch);
+/* Tile autotuner: centroid-window variant (0: 32, 1: 64, 2: 128 columns) the
+ * batched assignment uses for (d, k, float32); measured once, cached. */
+int kmc_tile_variant(int64_t n_features, int64_t n_clusters, kmc_stream_t stream,
+                     int *variant_out);
+/* Seeded synthetic Gaussian blobs written on the device, X_t (d, n). */
+int kmc_generate_blobs_f32(float *X_t, int64_t n_samples, int64_t n_features,
+                           int64_t n_centers, float box_lo, float box_hi, float std_lo,
+                           float std_hi, uint64_t seed, kmc_stream_t stream);
+/* Seeded distinct row indices for random-row initialisation (host). */
+int kmc_seeded_rows(int64_t n_samples, int64_t n_clusters, uint64_t seed, int32_t *rows_out);
+
+/* ---- serving loop ------------------------------------------------------------------
+ * No counterpart in the reference.  Replays a stream of fit and predict
+ * requests against the engine with continuous batching: a request is
+ * admitted at its arrival time as soon as an instance slot is free and the
+ * device bytes it needs fit the budget; running fits advance together one
+ * iteration per step; converged fits retire mid-batch and free their memory.
+ * Each request's data are seeded Gaussian blobs generated on the device at
+ * admission.  form KMC_FORM_PLAIN runs the batched engine; the mixed forms run
+ * one tensor-core fit session per request on a pool of streams.  Times are
+ * seconds from the start of the replay. */
+typedef struct {
+    double arrival_s;
+    int32_t kind;        /* 0 fit, 1 predict */
+    int32_t n_features;
+    int64_t n_samples;
+    int64_t n_clusters;
+    int64_t n_centers;   /* blobs of the request's data */
+    uint64_t seed;
+    double tol;
+    int64_t max_iter;
+    int64_t model;       /* predict: index of the fit request whose centroids it uses */
+    float std_lo, std_hi;
+} kmc_serve_request_t;
+typedef struct {
+    double admit_s;
+    double finish_s;
+    int64_t n_iter;
+    double inertia;
+    int32_t status;      /* KMC_OK or an error code */
+    int32_t pad;
+} kmc_serve_result_t;
+int kmc_serve_bytes_needed(int32_t kind, int64_t n_samples, int64_t n_features,
+                           int64_t n_clusters, int form, int64_t *bytes_out);
+int kmc_serve_run(const kmc_serve_request_t *requests, int64_t n_requests, int form,
+                  int64_t hbm_budget_bytes, int64_t max_active, kmc_stream_t stream,
+                  kmc_serve_result_t *results_out, double *makespan_s_out);
+
 /* ---- events: the (host_task_event, compute_event) pair of the reference ------------
  * The reference returns sycl::event pairs from every wrapper
  * (e.g. _kmeans_lloyd.cpp:102-103) and accepts `depends` lists.  These wrap

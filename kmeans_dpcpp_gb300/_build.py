@@ -43,8 +43,10 @@ CU_SOURCES = [
     "driver.cu",
     "capi.cu",
     "noalloc.cu",
+    "batch_kernels.cu",
+    "serve.cu",
 ]
-HEADERS = ["km_common.cuh", "km_kernels.cuh", "km_fit.cuh", "km_mixed.cuh"]
+HEADERS = ["km_common.cuh", "km_kernels.cuh", "km_fit.cuh", "km_mixed.cuh", "km_batch.cuh"]
 
 
 def _digest(paths, extra=""):

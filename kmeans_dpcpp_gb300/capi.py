@@ -21,12 +21,29 @@ _CTYPES = {
     "int": ctypes.c_int,
     "int64_t": ctypes.c_int64,
     "int32_t": ctypes.c_int32,
+    "uint64_t": ctypes.c_uint64,
     "double": ctypes.c_double,
     "float": ctypes.c_float,
     "void": None,
 }
 
 PRINT_FN = ctypes.CFUNCTYPE(None, ctypes.c_char_p, ctypes.c_void_p)
+
+
+class ServeRequest(ctypes.Structure):
+    """kmc_serve_request_t"""
+    _fields_ = [("arrival_s", ctypes.c_double), ("kind", ctypes.c_int32),
+                ("n_features", ctypes.c_int32), ("n_samples", ctypes.c_int64),
+                ("n_clusters", ctypes.c_int64), ("n_centers", ctypes.c_int64),
+                ("seed", ctypes.c_uint64), ("tol", ctypes.c_double), ("max_iter", ctypes.c_int64),
+                ("model", ctypes.c_int64), ("std_lo", ctypes.c_float), ("std_hi", ctypes.c_float)]
+
+
+class ServeResult(ctypes.Structure):
+    """kmc_serve_result_t"""
+    _fields_ = [("admit_s", ctypes.c_double), ("finish_s", ctypes.c_double),
+                ("n_iter", ctypes.c_int64), ("inertia", ctypes.c_double),
+                ("status", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 def _strip_comments(text: str) -> str:
@@ -56,7 +73,7 @@ def parse_header(path: str = HEADER):
 
 def _ctype(t: str):
     t = t.replace("const ", "").strip()
-    if t.endswith("*") or t in ("kmc_stream_t", "kmc_event_t", "kmc_fit_t"):
+    if t.endswith("*") or t in ("kmc_stream_t", "kmc_event_t", "kmc_fit_t", "kmc_batch_t"):
         if t == "char *" or t == "char*":
             return ctypes.c_char_p
         return ctypes.c_void_p

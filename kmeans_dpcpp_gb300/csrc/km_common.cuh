@@ -77,6 +77,8 @@ struct Scratch {
     Scratch(const Scratch &) = delete;
     Scratch &operator=(const Scratch &) = delete;
     int alloc(size_t bytes, cudaStream_t s) {
+        if (ptr) cudaFreeAsync(ptr, stream);  // re-allocation replaces the old block
+        ptr = nullptr;
         stream = s;
         if (bytes == 0) bytes = 16;
         cudaError_t e = cudaMallocAsync(&ptr, bytes, s);
@@ -87,9 +89,12 @@ struct Scratch {
         }
         return KMC_OK;
     }
-    ~Scratch() {
+    // Stream-ordered free now (the object can be re-used).
+    void release() {
         if (ptr) cudaFreeAsync(ptr, stream);
+        ptr = nullptr;
     }
+    ~Scratch() { release(); }
     template <typename U> U *as() const { return static_cast<U *>(ptr); }
 };
 

@@ -1,0 +1,794 @@
+// Host side of the batched Lloyd engine (km_batch.cuh) and the serving loop,
+// with their extern "C" entry points (include/kmeans_gb300.h).
+//
+// BatchEngine::step() advances every running instance by one iteration:
+//   graph A   batch_prep -> batch_assign (one launch per centroid-window
+//             variant in use, all fed from the device work queue) ->
+//             batch_reduce
+//   host      reads the empty-cluster counts of the fitting instances; those
+//             with empty clusters run the single-fit relocation chain
+//             (kmeans_lloyd_driver.hpp:217-312) on their own buffers
+//   graph B   batch_update (divide, shifts, stop rule, copy-back)
+//   host      reads the stop flags; finished fits get the driver's final pass
+//             (half norms, assignment, weighted inertia, float64 total,
+//             kmeans_lloyd_driver.hpp:360-418); predictions finish after
+//             their assignment
+// The two graphs are captured once per set of running instances and replayed
+// until an instance joins or leaves.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <thread>
+#include <vector>
+
+#include "km_batch.cuh"
+#include "kmeans_gb300.h"
+
+namespace kmc {
+
+namespace {
+
+constexpr int kItemTiles = 8;  // 128-sample tiles per work item
+
+// Engine-owned device memory of one instance.
+struct SlotMem {
+    Scratch mem;
+    float *Cn = nullptr, *hn = nullptr, *sizes = nullptr, *sq_dist = nullptr, *thr = nullptr;
+    double *sums = nullptr, *partials = nullptr, *dsum = nullptr;
+    int32_t *empty_list = nullptr, *selected = nullptr;
+    void *thr_scratch = nullptr, *sel_scratch = nullptr;
+};
+
+size_t slot_bytes(int mode, int64_t n, int64_t d, int64_t k) {
+    size_t b = align256(sizeof(float) * d * k) + 2 * align256(sizeof(float) * k);
+    if (mode == B_FIT) {
+        b += align256(sizeof(double) * (d * k + k)) + align256(sizeof(int32_t) * (k + 1)) +
+             align256(sizeof(float) * n) + align256(sizeof(int32_t) * (n + 2)) +
+             align256(sizeof(float)) + align256(threshold_scratch_bytes()) +
+             align256(select_scratch_bytes(k)) + align256(sizeof(double) * sum_partials_size()) +
+             align256(sizeof(double));
+    }
+    return b;
+}
+
+int alloc_slot(SlotMem &m, int mode, int64_t n, int64_t d, int64_t k, cudaStream_t s) {
+    KMC_TRY(m.mem.alloc(slot_bytes(mode, n, d, k), s));
+    char *b = m.mem.as<char>();
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char *p = b + off;
+        off += align256(bytes);
+        return p;
+    };
+    m.Cn = reinterpret_cast<float *>(take(sizeof(float) * d * k));
+    m.hn = reinterpret_cast<float *>(take(sizeof(float) * k));
+    m.sizes = reinterpret_cast<float *>(take(sizeof(float) * k));
+    if (mode == B_FIT) {
+        m.sums = reinterpret_cast<double *>(take(sizeof(double) * (d * k + k)));
+        m.empty_list = reinterpret_cast<int32_t *>(take(sizeof(int32_t) * (k + 1)));
+        m.sq_dist = reinterpret_cast<float *>(take(sizeof(float) * n));
+        m.selected = reinterpret_cast<int32_t *>(take(sizeof(int32_t) * (n + 2)));
+        m.thr = reinterpret_cast<float *>(take(sizeof(float)));
+        m.thr_scratch = take(threshold_scratch_bytes());
+        m.sel_scratch = take(select_scratch_bytes(k));
+        m.partials = reinterpret_cast<double *>(take(sizeof(double) * sum_partials_size()));
+        m.dsum = reinterpret_cast<double *>(take(sizeof(double)));
+    }
+    return KMC_OK;
+}
+
+struct GraphExec {
+    cudaGraphExec_t exec = nullptr;
+    ~GraphExec() { reset(); }
+    void reset() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+    }
+};
+
+}  // namespace
+
+struct BatchEngine {
+    enum SlotState { FREE = 0, RUNNING = 1, FINISHED = 2 };
+    // The engine's work runs on its own stream (graphs cannot capture the
+    // legacy default stream); events order it after the caller's stream when
+    // instances are added and the caller's stream after each step.
+    cudaStream_t user = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    int64_t cap = 0;
+    Scratch dev;                    // table, lists, work queue, counters, status
+    BInst *tab_d = nullptr;
+    int *all_d = nullptr, *fit_d = nullptr, *counters_d = nullptr;
+    int *nempty_d = nullptr, *done_d = nullptr;
+    BItem *items_d = nullptr;
+    int64_t items_cap = 0;
+    Scratch items_mem;
+    std::vector<BInst> tab;
+    std::vector<int> state;
+    std::vector<std::unique_ptr<SlotMem>> mem;
+    std::vector<long long> res_iter;
+    std::vector<double> res_inertia;
+    // current step plan
+    std::vector<int> all, fits;
+    int n_items[kBatchVariants] = {0, 0, 0};
+    int64_t item_off[kBatchVariants] = {0, 0, 0};
+    bool dirty = true;
+    GraphExec gA, gB;
+    int *host_i = nullptr;  // pinned: empty counts then done flags
+    int64_t steps = 0, graph_builds = 0, relocations = 0;
+
+    ~BatchEngine() {
+        if (s) cudaStreamSynchronize(s);
+        if (host_i) cudaFreeHost(host_i);
+        // device memory is released (stream-ordered) before the stream goes
+        gA.reset();
+        gB.reset();
+        mem.clear();
+        items_mem.release();
+        dev.release();
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+        if (ev_in) cudaEventDestroy(ev_in);
+        if (ev_out) cudaEventDestroy(ev_out);
+    }
+
+    int init(int64_t capacity, cudaStream_t stream) {
+        KMC_CHECK_ARG(capacity > 0 && capacity <= (1 << 20), "max_instances out of range");
+        user = stream;
+        KMC_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        KMC_CUDA_TRY(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
+        KMC_CUDA_TRY(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
+        cap = capacity;
+        const size_t o_tab = 0;
+        const size_t o_all = o_tab + align256(sizeof(BInst) * cap);
+        const size_t o_fit = o_all + align256(sizeof(int) * cap);
+        const size_t o_cnt = o_fit + align256(sizeof(int) * cap);
+        const size_t o_ne = o_cnt + align256(sizeof(int) * kBatchVariants);
+        const size_t o_dn = o_ne + align256(sizeof(int) * cap);
+        KMC_TRY(dev.alloc(o_dn + align256(sizeof(int) * cap), s));
+        char *b = dev.as<char>();
+        tab_d = reinterpret_cast<BInst *>(b + o_tab);
+        all_d = reinterpret_cast<int *>(b + o_all);
+        fit_d = reinterpret_cast<int *>(b + o_fit);
+        counters_d = reinterpret_cast<int *>(b + o_cnt);
+        nempty_d = reinterpret_cast<int *>(b + o_ne);
+        done_d = reinterpret_cast<int *>(b + o_dn);
+        KMC_CUDA_TRY(cudaMallocHost(&host_i, sizeof(int) * 2 * cap));
+        tab.assign((size_t)cap, BInst{});
+        state.assign((size_t)cap, FREE);
+        mem.resize((size_t)cap);
+        res_iter.assign((size_t)cap, 0);
+        res_inertia.assign((size_t)cap, 0.0);
+        return KMC_OK;
+    }
+
+    int free_slot(int64_t *slot) {
+        for (int64_t q = 0; q < cap; ++q)
+            if (state[(size_t)q] == FREE) {
+                *slot = q;
+                return KMC_OK;
+            }
+        set_error("all %lld instance slots are in use", (long long)cap);
+        return KMC_ERR_UNSUPPORTED;
+    }
+
+    int upload(int64_t q) {
+        KMC_CUDA_TRY(cudaMemcpyAsync(tab_d + q, &tab[(size_t)q], sizeof(BInst),
+                                     cudaMemcpyHostToDevice, s));
+        // the host copy may change before the copy runs: order it now
+        KMC_CUDA_TRY(cudaStreamSynchronize(s));
+        return KMC_OK;
+    }
+
+    int add(int mode, const float *X, const float *w, float *C, int32_t *labels, int64_t n,
+            int64_t d, int64_t k, double tol, int64_t max_iter, int64_t *out) {
+        KMC_CHECK_ARG(n >= 0 && d >= 1 && k >= 1, "invalid dimensions (n=%lld, d=%lld, k=%lld)",
+                      (long long)n, (long long)d, (long long)k);
+        KMC_CHECK_ARG(d <= 1024 && k <= 4096, "batched fits take d <= 1024 and k <= 4096");
+        KMC_CHECK_ARG(n < (int64_t(1) << 31), "n_samples must fit int32 labels");
+        KMC_CHECK_ARG(mode == B_ASSIGN || k <= n, "n_clusters exceeds n_samples");
+        KMC_CHECK_ARG(tol >= 0.0, "Tolerance must be non-negative");
+        int64_t q = 0;
+        KMC_TRY(free_slot(&q));
+        // the caller's writes of X, w and C come first
+        KMC_CUDA_TRY(cudaEventRecord(ev_in, user));
+        KMC_CUDA_TRY(cudaStreamWaitEvent(s, ev_in, 0));
+        auto m = std::make_unique<SlotMem>();
+        KMC_TRY(alloc_slot(*m, mode, n, d, k, s));
+        int variant = 2;
+        KMC_TRY(tune_variant(d, k, s, &variant));
+        BInst h{};
+        h.X = X;
+        h.w = w;
+        h.C = C;
+        h.Cn = m->Cn;
+        h.hn = m->hn;
+        h.sizes = m->sizes;
+        h.sums = m->sums;
+        h.labels = labels;
+        h.empty_list = m->empty_list;
+        h.n = n;
+        h.d = (int)d;
+        h.k = (int)k;
+        h.mode = mode;
+        h.variant = variant;
+        h.st.max_iter = max_iter;
+        const float tol_t = (float)tol;
+        h.st.tol = (double)tol_t;
+        // while (n_iter < max_iter && shift_sum > tol), shift_sum = +inf at
+        // the start (kmeans_lloyd_driver.hpp:78, 83)
+        h.st.done = (mode == B_FIT && !(0 < max_iter && pos_inf<float>() > tol_t)) ? 1 : 0;
+        tab[(size_t)q] = h;
+        mem[(size_t)q] = std::move(m);
+        state[(size_t)q] = RUNNING;
+        res_iter[(size_t)q] = 0;
+        res_inertia[(size_t)q] = 0.0;
+        KMC_TRY(upload(q));
+        dirty = true;
+        *out = q;
+        if (h.st.done) KMC_TRY(finish_fit(q));
+        return KMC_OK;
+    }
+
+    int remove(int64_t q) {
+        KMC_CHECK_ARG(q >= 0 && q < cap && state[(size_t)q] != FREE, "no such instance");
+        KMC_CUDA_TRY(cudaStreamSynchronize(s));
+        mem[(size_t)q].reset();
+        state[(size_t)q] = FREE;
+        dirty = true;
+        return KMC_OK;
+    }
+
+    int64_t running() const {
+        int64_t c = 0;
+        for (int v : state) c += (v == RUNNING);
+        return c;
+    }
+
+    // Work lists, work queue and graphs for the current running set.
+    int plan() {
+        all.clear();
+        fits.clear();
+        std::vector<BItem> items[kBatchVariants];
+        for (int64_t q = 0; q < cap; ++q) {
+            if (state[(size_t)q] != RUNNING) continue;
+            const BInst &h = tab[(size_t)q];
+            all.push_back((int)q);
+            if (h.mode == B_FIT) fits.push_back((int)q);
+            const int64_t tiles = ceil_div<int64_t>(h.n, kBatchTileM);
+            for (int64_t t = 0; t < tiles; t += kItemTiles)
+                items[h.variant].push_back(
+                    BItem{(int)q, (int)std::min<int64_t>(kItemTiles, tiles - t), (long long)t});
+        }
+        int64_t total = 0;
+        for (int v = 0; v < kBatchVariants; ++v) {
+            item_off[v] = total;
+            n_items[v] = (int)items[v].size();
+            total += n_items[v];
+        }
+        if (total > items_cap) {
+            items_cap = std::max<int64_t>(total, 2 * items_cap);
+            KMC_TRY(items_mem.alloc(sizeof(BItem) * (size_t)items_cap, s));
+            items_d = items_mem.as<BItem>();
+        }
+        for (int v = 0; v < kBatchVariants; ++v)
+            if (n_items[v] > 0)
+                KMC_CUDA_TRY(cudaMemcpyAsync(items_d + item_off[v], items[v].data(),
+                                             sizeof(BItem) * n_items[v], cudaMemcpyHostToDevice,
+                                             s));
+        if (!all.empty())
+            KMC_CUDA_TRY(cudaMemcpyAsync(all_d, all.data(), sizeof(int) * all.size(),
+                                         cudaMemcpyHostToDevice, s));
+        if (!fits.empty())
+            KMC_CUDA_TRY(cudaMemcpyAsync(fit_d, fits.data(), sizeof(int) * fits.size(),
+                                         cudaMemcpyHostToDevice, s));
+        KMC_CUDA_TRY(cudaStreamSynchronize(s));
+        // kernel attributes are set outside the capture
+        KMC_TRY(prepare_batch_assign());
+        KMC_TRY(capture(&gA, [&]() -> int {
+            KMC_TRY(launch_batch_prep(tab_d, all_d, (int)all.size(), counters_d, s));
+            for (int v = 0; v < kBatchVariants; ++v)
+                KMC_TRY(launch_batch_assign(v, tab_d, items_d + item_off[v], n_items[v],
+                                            counters_d + v, s));
+            return launch_batch_reduce(tab_d, fit_d, (int)fits.size(), nempty_d, s);
+        }));
+        KMC_TRY(capture(&gB, [&]() -> int {
+            return launch_batch_update(tab_d, fit_d, (int)fits.size(), done_d, s);
+        }));
+        ++graph_builds;
+        dirty = false;
+        return KMC_OK;
+    }
+
+    template <typename F>
+    int capture(GraphExec *g, F body) {
+        g->reset();
+        cudaGraph_t graph = nullptr;
+        KMC_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const int rc = body();
+        const cudaError_t e = cudaStreamEndCapture(s, &graph);
+        if (rc != KMC_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        KMC_CUDA_TRY(e);
+        const cudaError_t ei = cudaGraphInstantiate(&g->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        KMC_CUDA_TRY(ei);
+        return KMC_OK;
+    }
+
+    // kmeans_lloyd_driver.hpp:217-312 for one instance with m empty clusters.
+    int relocate(int64_t q, int m) {
+        const BInst &h = tab[(size_t)q];
+        SlotMem &sm = *mem[(size_t)q];
+        int32_t *counters = sm.selected + h.n;
+        KMC_TRY(launch_inertia<float, int32_t>(h.X, nullptr, h.C, h.labels, sm.sq_dist, h.n, h.d,
+                                               h.k, s));
+        KMC_TRY(launch_threshold<float>(sm.sq_dist, h.n, nullptr, m, sm.thr, sm.thr_scratch, s));
+        KMC_TRY(launch_fill<int32_t>(counters, 0, 1, s));
+        KMC_TRY(launch_fill<int32_t>(counters + 1, 1, 1, s));
+        KMC_TRY(launch_select<float, int32_t>(nullptr, m, sm.sq_dist, sm.thr, sm.selected,
+                                              counters, counters + 1, h.n, sm.sel_scratch, s));
+        KMC_TRY(launch_relocate<float, int32_t>(nullptr, m, h.X, h.w, h.labels, sm.selected,
+                                                counters, sm.empty_list, sm.Cn, sm.sizes,
+                                                sm.sq_dist, h.n, h.d, h.k, s));
+        ++relocations;
+        return KMC_OK;
+    }
+
+    // kmeans_lloyd_driver.hpp:360-418: labels and weighted inertia against
+    // the final centroids.
+    int finish_fit(int64_t q) {
+        const BInst &h = tab[(size_t)q];
+        SlotMem &sm = *mem[(size_t)q];
+        KMC_TRY(launch_half_norm<float>(h.C, sm.hn, h.d, h.k, s));
+        KMC_TRY(launch_assignment<float, int32_t>(h.X, h.C, sm.hn, h.labels, h.n, h.d, h.k, s));
+        KMC_TRY(launch_inertia<float, int32_t>(h.X, h.w, h.C, h.labels, sm.sq_dist, h.n, h.d,
+                                               h.k, s));
+        KMC_TRY(launch_sum_f64<float>(sm.sq_dist, h.n, sm.partials, sm.dsum, s));
+        LoopState st{};
+        double tot = 0.0;
+        KMC_CUDA_TRY(cudaMemcpyAsync(&st, &tab_d[q].st, sizeof(st), cudaMemcpyDeviceToHost, s));
+        KMC_CUDA_TRY(cudaMemcpyAsync(&tot, sm.dsum, sizeof(double), cudaMemcpyDeviceToHost, s));
+        KMC_CUDA_TRY(cudaStreamSynchronize(s));
+        res_iter[(size_t)q] = st.n_iter;
+        res_inertia[(size_t)q] = tot;
+        state[(size_t)q] = FINISHED;
+        dirty = true;
+        return KMC_OK;
+    }
+
+    int step(int64_t *n_active) {
+        if (dirty) KMC_TRY(plan());
+        if (!all.empty()) {
+            KMC_CUDA_TRY(cudaGraphLaunch(gA.exec, s));
+            const size_t nf = fits.size();
+            if (nf > 0) {
+                KMC_CUDA_TRY(cudaMemcpyAsync(host_i, nempty_d, sizeof(int) * nf,
+                                             cudaMemcpyDeviceToHost, s));
+                KMC_CUDA_TRY(cudaStreamSynchronize(s));
+                for (size_t t = 0; t < nf; ++t)
+                    if (host_i[t] > 0) KMC_TRY(relocate(fits[t], host_i[t]));
+                KMC_CUDA_TRY(cudaGraphLaunch(gB.exec, s));
+                KMC_CUDA_TRY(cudaMemcpyAsync(host_i + cap, done_d, sizeof(int) * nf,
+                                             cudaMemcpyDeviceToHost, s));
+            }
+            KMC_CUDA_TRY(cudaStreamSynchronize(s));
+            ++steps;
+            for (size_t t = 0; t < nf; ++t)
+                if (host_i[cap + t]) KMC_TRY(finish_fit(fits[t]));
+            for (int q : all)
+                if (tab[(size_t)q].mode == B_ASSIGN) {
+                    state[(size_t)q] = FINISHED;
+                    res_iter[(size_t)q] = 0;
+                    dirty = true;
+                }
+        }
+        KMC_CUDA_TRY(cudaEventRecord(ev_out, s));
+        KMC_CUDA_TRY(cudaStreamWaitEvent(user, ev_out, 0));
+        if (n_active) *n_active = running();
+        return KMC_OK;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Serving loop
+// ---------------------------------------------------------------------------
+namespace {
+
+// Device bytes one request holds while admitted (its data, centroids and
+// labels, plus the engine's or the fit session's working memory).
+int64_t request_bytes(int kind, int64_t n, int64_t d, int64_t k, int form) {
+    const int64_t d4 = ceil_div<int64_t>(std::max<int64_t>(d, 1), 4) * 4;
+    int64_t b = (int64_t)(align256(sizeof(float) * n * d) + align256(sizeof(float) * n) +
+                          align256(sizeof(float) * d * k) + align256(sizeof(int32_t) * n));
+    if (form == KMC_FORM_PLAIN) {
+        b += (int64_t)slot_bytes(kind == 0 ? B_FIT : B_ASSIGN, n, d, k);
+    } else {
+        // plain-fit workspace plus the tensor-core operands: fp16/bf16 image,
+        // fp32 row copy, norms, candidate masks, recheck list, cluster sums
+        const int64_t nkb = ceil_div<int64_t>(std::max<int64_t>(d, 1), 64);
+        const int64_t kp = ceil_div<int64_t>(k, 256) * 256;
+        b += (int64_t)slot_bytes(B_FIT, n, d, k) +
+             n * (nkb * 128 + 4 * d4 + 8 + 16 + 4) + kp * (nkb * 128 + 32 + 4 * d4) +
+             152 * (kp * d4 + kp) * 8;
+    }
+    return b + (b >> 4) + (16 << 20);  // allocator slack
+}
+
+struct ReqMem {
+    Scratch mem;
+    float *X = nullptr, *w = nullptr, *C = nullptr, *Cres = nullptr;
+    int32_t *labels = nullptr;
+};
+
+int alloc_request(ReqMem &m, int64_t n, int64_t d, int64_t k, cudaStream_t s) {
+    const size_t bX = align256(sizeof(float) * n * d), bw = align256(sizeof(float) * n),
+                 bC = align256(sizeof(float) * d * k), bl = align256(sizeof(int32_t) * n);
+    KMC_TRY(m.mem.alloc(bX + bw + 2 * bC + bl, s));
+    char *b = m.mem.as<char>();
+    m.X = reinterpret_cast<float *>(b);
+    m.w = reinterpret_cast<float *>(b + bX);
+    m.C = reinterpret_cast<float *>(b + bX + bw);
+    m.Cres = reinterpret_cast<float *>(b + bX + bw + bC);
+    m.labels = reinterpret_cast<int32_t *>(b + bX + bw + 2 * bC);
+    return KMC_OK;
+}
+
+struct Active {
+    int64_t req = -1;
+    int64_t inst = -1;                 // plain: batch instance
+    std::unique_ptr<FitBase> fit;      // mixed: tensor-core fit session
+    int stream = 0;
+    int64_t bytes = 0;
+    std::unique_ptr<ReqMem> mem;
+};
+
+int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t budget,
+              int64_t max_active, cudaStream_t s, kmc_serve_result_t *out, double *makespan) {
+    KMC_CHECK_ARG(n_req >= 0 && (n_req == 0 || (rq != nullptr && out != nullptr)),
+                  "null request or result array");
+    KMC_CHECK_ARG(max_active >= 1, "max_active must be positive");
+    KMC_CHECK_ARG(form == KMC_FORM_PLAIN || form == KMC_FORM_MIXED_BF16 ||
+                      form == KMC_FORM_MIXED_FP16,
+                  "unknown form %d", form);
+    for (int64_t r = 0; r < n_req; ++r) {
+        const kmc_serve_request_t &q = rq[r];
+        KMC_CHECK_ARG(q.kind == 0 || q.kind == 1, "request %lld: kind must be 0 or 1",
+                      (long long)r);
+        KMC_CHECK_ARG(q.n_samples >= 1 && q.n_features >= 1 && q.n_clusters >= 1 &&
+                          (q.kind == 1 || q.n_clusters <= q.n_samples) && q.n_centers >= 1,
+                      "request %lld: invalid sizes", (long long)r);
+        KMC_CHECK_ARG(r == 0 || q.arrival_s >= rq[r - 1].arrival_s,
+                      "requests must be sorted by arrival time");
+        KMC_CHECK_ARG(q.kind == 0 || (q.model >= 0 && q.model < r && rq[q.model].kind == 0 &&
+                                      rq[q.model].n_features == q.n_features &&
+                                      rq[q.model].n_clusters == q.n_clusters),
+                      "request %lld: a prediction must name an earlier fit of the same d, k",
+                      (long long)r);
+        out[r] = kmc_serve_result_t{-1.0, -1.0, 0, 0.0, KMC_OK, 0};
+    }
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    auto elapsed = [&]() { return std::chrono::duration<double>(clk::now() - t0).count(); };
+
+    const bool plain = form == KMC_FORM_PLAIN;
+    BatchEngine eng;
+    if (plain) KMC_TRY(eng.init(max_active, s));
+    constexpr int kStreams = 8;
+    std::vector<cudaStream_t> pool;
+    if (!plain) {
+        for (int q = 0; q < kStreams; ++q) {
+            cudaStream_t t = nullptr;
+            KMC_CUDA_TRY(cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking));
+            pool.push_back(t);
+        }
+    }
+    struct PoolGuard {
+        std::vector<cudaStream_t> &p;
+        ~PoolGuard() {
+            for (auto t : p) {
+                cudaStreamSynchronize(t);
+                cudaStreamDestroy(t);
+            }
+        }
+    } pool_guard{pool};
+
+    std::vector<std::vector<float>> models((size_t)n_req);
+    std::vector<char> model_ready((size_t)n_req, 0);
+    std::deque<int64_t> pending;
+    std::vector<std::unique_ptr<Active>> active;
+    int64_t next = 0, finished = 0, in_use = 0, rr = 0;
+
+    auto finish = [&](Active &a, int64_t n_iter, double inertia, int status) -> int {
+        const kmc_serve_request_t &q = rq[a.req];
+        kmc_serve_result_t &o = out[a.req];
+        if (status == KMC_OK && q.kind == 0) {
+            std::vector<float> &m = models[(size_t)a.req];
+            m.resize((size_t)(q.n_features * q.n_clusters));
+            const float *src = plain ? a.mem->C : a.mem->Cres;
+            KMC_CUDA_TRY(cudaMemcpy(m.data(), src, sizeof(float) * m.size(),
+                                    cudaMemcpyDeviceToHost));
+            model_ready[(size_t)a.req] = 1;
+        }
+        o.finish_s = elapsed();
+        o.n_iter = n_iter;
+        o.inertia = inertia;
+        o.status = status;
+        in_use -= a.bytes;
+        ++finished;
+        return KMC_OK;
+    };
+
+    auto admit = [&](int64_t r, int64_t bytes) -> int {
+        const kmc_serve_request_t &q = rq[r];
+        auto a = std::make_unique<Active>();
+        a->req = r;
+        a->bytes = bytes;
+        a->mem = std::make_unique<ReqMem>();
+        const int64_t n = q.n_samples, d = q.n_features, k = q.n_clusters;
+        cudaStream_t st = plain ? s : pool[(size_t)(rr++ % kStreams)];
+        a->stream = plain ? 0 : (int)((rr - 1) % kStreams);
+        KMC_TRY(alloc_request(*a->mem, n, d, k, st));
+        ReqMem &m = *a->mem;
+        KMC_TRY(launch_blobs(m.X, n, d, q.n_centers, -10.f, 10.f, q.std_lo, q.std_hi, q.seed, st));
+        KMC_TRY(launch_fill<float>(m.w, 1.f, n, st));
+        if (q.kind == 0) {
+            std::vector<int32_t> rows;
+            seeded_rows(n, k, q.seed ^ 0x9999ull, &rows);
+            Scratch idx;
+            KMC_TRY(idx.alloc(sizeof(int32_t) * rows.size(), st));
+            KMC_CUDA_TRY(cudaMemcpyAsync(idx.ptr, rows.data(), sizeof(int32_t) * rows.size(),
+                                         cudaMemcpyHostToDevice, st));
+            KMC_TRY(launch_gather_rows(m.X, n, d, idx.as<int32_t>(), k, m.C, st));
+            KMC_CUDA_TRY(cudaStreamSynchronize(st));
+        } else {
+            const std::vector<float> &mdl = models[(size_t)q.model];
+            KMC_CUDA_TRY(cudaMemcpyAsync(m.C, mdl.data(), sizeof(float) * mdl.size(),
+                                         cudaMemcpyHostToDevice, st));
+            KMC_CUDA_TRY(cudaStreamSynchronize(st));
+        }
+        out[r].admit_s = elapsed();
+        if (plain) {
+            if (q.kind == 0)
+                KMC_TRY(eng.add(B_FIT, m.X, m.w, m.C, m.labels, n, d, k, q.tol, q.max_iter,
+                                &a->inst));
+            else
+                KMC_TRY(eng.add(B_ASSIGN, m.X, nullptr, m.C, m.labels, n, d, k, 0.0, 0, &a->inst));
+        } else {
+            FitParams<float, int32_t> p;
+            p.X = m.X;
+            p.w = m.w;
+            p.centroids = m.C;
+            p.new_centroids = m.Cres;
+            p.labels = m.labels;
+            p.n = n;
+            p.d = d;
+            p.k = k;
+            p.tol = q.kind == 0 ? q.tol : 0.0;
+            p.max_iter = q.kind == 0 ? q.max_iter : 0;
+            p.stream = st;
+            KMC_TRY(make_mixed_fit<float, int32_t>(p, form, &a->fit));
+        }
+        in_use += bytes;
+        active.push_back(std::move(a));
+        return KMC_OK;
+    };
+
+    while (finished < n_req) {
+        const double now = elapsed();
+        while (next < n_req && rq[next].arrival_s <= now) pending.push_back(next++);
+        // admission in arrival order; predictions wait (without blocking the
+        // queue) until their model has been fitted
+        for (auto it = pending.begin(); it != pending.end();) {
+            const kmc_serve_request_t &q = rq[*it];
+            if (q.kind == 1 && !model_ready[(size_t)q.model]) {
+                ++it;
+                continue;
+            }
+            const int64_t need = request_bytes(q.kind, q.n_samples, q.n_features, q.n_clusters,
+                                               form);
+            if (need > budget) {  // can never be admitted
+                out[*it].status = KMC_ERR_OUT_OF_MEMORY;
+                out[*it].finish_s = elapsed();
+                ++finished;
+                it = pending.erase(it);
+                continue;
+            }
+            if ((int64_t)active.size() >= max_active || in_use + need > budget) break;
+            KMC_TRY(admit(*it, need));
+            it = pending.erase(it);
+        }
+        if (active.empty()) {
+            if (next < n_req) {
+                const double wait = rq[next].arrival_s - elapsed();
+                if (wait > 0)
+                    std::this_thread::sleep_for(
+                        std::chrono::microseconds((int64_t)(std::min(wait, 0.001) * 1e6)));
+            } else if (!pending.empty()) {
+                // only predictions whose model failed remain
+                for (int64_t r : pending) {
+                    out[r].status = KMC_ERR_INVALID_ARGUMENT;
+                    out[r].finish_s = elapsed();
+                    ++finished;
+                }
+                pending.clear();
+            }
+            continue;
+        }
+        if (plain) {
+            KMC_TRY(eng.step(nullptr));
+            for (size_t t = 0; t < active.size();) {
+                Active &a = *active[t];
+                if (eng.state[(size_t)a.inst] == BatchEngine::FINISHED) {
+                    KMC_TRY(finish(a, eng.res_iter[(size_t)a.inst], eng.res_inertia[(size_t)a.inst],
+                                   KMC_OK));
+                    KMC_TRY(eng.remove(a.inst));
+                    active.erase(active.begin() + (int64_t)t);
+                } else {
+                    ++t;
+                }
+            }
+        } else {
+            // one iteration of every running session, overlapped across streams
+            std::vector<int> was_done(active.size(), 0);
+            for (size_t t = 0; t < active.size(); ++t) {
+                LoopState st{};
+                KMC_TRY(active[t]->fit->read_state(st));
+                was_done[t] = st.done;
+                if (!st.done) KMC_TRY(active[t]->fit->enqueue_iteration());
+            }
+            for (size_t t = 0; t < active.size();) {
+                Active &a = *active[t];
+                LoopState st{};
+                KMC_TRY(a.fit->read_state(st));
+                if (st.done) {
+                    int64_t it = 0;
+                    double inertia = 0.0;
+                    KMC_TRY(a.fit->finalize(&it, &inertia));
+                    KMC_TRY(finish(a, it, inertia, KMC_OK));
+                    a.fit.reset();
+                    active.erase(active.begin() + (int64_t)t);
+                } else {
+                    ++t;
+                }
+            }
+            (void)was_done;
+        }
+    }
+    if (makespan) *makespan = elapsed();
+    return KMC_OK;
+}
+
+}  // namespace
+
+}  // namespace kmc
+
+using namespace kmc;
+
+struct kmc_batch_s {
+    BatchEngine eng;
+};
+
+extern "C" {
+
+int kmc_batch_create(int64_t max_instances, kmc_stream_t stream, kmc_batch_t *batch_out) {
+    KMC_CHECK_ARG(batch_out != nullptr, "null output handle");
+    auto b = std::make_unique<kmc_batch_s>();
+    KMC_TRY(b->eng.init(max_instances, reinterpret_cast<cudaStream_t>(stream)));
+    *batch_out = b.release();
+    return KMC_OK;
+}
+
+int kmc_batch_add_fit_f32(kmc_batch_t batch, const float *X_t, const float *sample_weight,
+                          float *centroids_t, int32_t *labels, int64_t n_samples,
+                          int64_t n_features, int64_t n_clusters, double tol, int64_t max_iter,
+                          int64_t *instance_out) {
+    KMC_CHECK_ARG(batch != nullptr && instance_out != nullptr, "null argument");
+    KMC_CHECK_ARG(max_iter >= 0, "max_iter must be non-negative");
+    return batch->eng.add(B_FIT, X_t, sample_weight, centroids_t, labels, n_samples, n_features,
+                          n_clusters, tol, max_iter, instance_out);
+}
+
+int kmc_batch_add_predict_f32(kmc_batch_t batch, const float *X_t, const float *centroids_t,
+                              int32_t *labels, int64_t n_samples, int64_t n_features,
+                              int64_t n_clusters, int64_t *instance_out) {
+    KMC_CHECK_ARG(batch != nullptr && instance_out != nullptr, "null argument");
+    return batch->eng.add(B_ASSIGN, X_t, nullptr, const_cast<float *>(centroids_t), labels,
+                          n_samples, n_features, n_clusters, 0.0, 0, instance_out);
+}
+
+int kmc_batch_step(kmc_batch_t batch, int64_t *n_active_out) {
+    KMC_CHECK_ARG(batch != nullptr, "null batch");
+    return batch->eng.step(n_active_out);
+}
+
+int kmc_batch_run(kmc_batch_t batch) {
+    KMC_CHECK_ARG(batch != nullptr, "null batch");
+    int64_t active = 1;
+    while (active > 0) KMC_TRY(batch->eng.step(&active));
+    return KMC_OK;
+}
+
+int kmc_batch_result(kmc_batch_t batch, int64_t instance, int *finished_out,
+                     int64_t *n_iter_out, double *inertia_out) {
+    KMC_CHECK_ARG(batch != nullptr, "null batch");
+    BatchEngine &e = batch->eng;
+    KMC_CHECK_ARG(instance >= 0 && instance < e.cap && e.state[(size_t)instance] != 0,
+                  "no such instance");
+    if (finished_out) *finished_out = e.state[(size_t)instance] == BatchEngine::FINISHED;
+    if (n_iter_out) *n_iter_out = e.res_iter[(size_t)instance];
+    if (inertia_out) *inertia_out = e.res_inertia[(size_t)instance];
+    return KMC_OK;
+}
+
+int kmc_batch_remove(kmc_batch_t batch, int64_t instance) {
+    KMC_CHECK_ARG(batch != nullptr, "null batch");
+    return batch->eng.remove(instance);
+}
+
+int kmc_batch_stats(kmc_batch_t batch, int64_t *steps_out, int64_t *graph_builds_out,
+                    int64_t *relocations_out) {
+    KMC_CHECK_ARG(batch != nullptr, "null batch");
+    if (steps_out) *steps_out = batch->eng.steps;
+    if (graph_builds_out) *graph_builds_out = batch->eng.graph_builds;
+    if (relocations_out) *relocations_out = batch->eng.relocations;
+    return KMC_OK;
+}
+
+int kmc_batch_destroy(kmc_batch_t batch) {
+    if (batch == nullptr) return KMC_OK;
+    cudaStreamSynchronize(batch->eng.s);
+    delete batch;
+    return KMC_OK;
+}
+
+int kmc_tile_variant(int64_t n_features, int64_t n_clusters, kmc_stream_t stream,
+                     int *variant_out) {
+    KMC_CHECK_ARG(variant_out != nullptr, "null output");
+    KMC_CHECK_ARG(n_features >= 1 && n_features <= 1024 && n_clusters >= 1 && n_clusters <= 4096,
+                  "n_features / n_clusters out of range");
+    return tune_variant(n_features, n_clusters, reinterpret_cast<cudaStream_t>(stream),
+                        variant_out);
+}
+
+int kmc_generate_blobs_f32(float *X_t, int64_t n_samples, int64_t n_features,
+                           int64_t n_centers, float box_lo, float box_hi, float std_lo,
+                           float std_hi, uint64_t seed, kmc_stream_t stream) {
+    KMC_CHECK_ARG(n_samples >= 0 && n_features >= 0, "negative dimension");
+    return launch_blobs(X_t, n_samples, n_features, n_centers, box_lo, box_hi, std_lo, std_hi,
+                        seed, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int kmc_seeded_rows(int64_t n_samples, int64_t n_clusters, uint64_t seed, int32_t *rows_out) {
+    KMC_CHECK_ARG(rows_out != nullptr, "null output");
+    KMC_CHECK_ARG(n_clusters >= 0 && n_clusters <= n_samples, "n_clusters exceeds n_samples");
+    std::vector<int32_t> r;
+    seeded_rows(n_samples, n_clusters, seed, &r);
+    std::memcpy(rows_out, r.data(), sizeof(int32_t) * r.size());
+    return KMC_OK;
+}
+
+int kmc_serve_bytes_needed(int32_t kind, int64_t n_samples, int64_t n_features,
+                           int64_t n_clusters, int form, int64_t *bytes_out) {
+    KMC_CHECK_ARG(bytes_out != nullptr, "null output");
+    KMC_CHECK_ARG(kind == 0 || kind == 1, "kind must be 0 (fit) or 1 (predict)");
+    KMC_CHECK_ARG(n_samples >= 0 && n_features >= 1 && n_clusters >= 1, "invalid sizes");
+    *bytes_out = request_bytes(kind, n_samples, n_features, n_clusters, form);
+    return KMC_OK;
+}
+
+int kmc_serve_run(const kmc_serve_request_t *requests, int64_t n_requests, int form,
+                  int64_t hbm_budget_bytes, int64_t max_active, kmc_stream_t stream,
+                  kmc_serve_result_t *results_out, double *makespan_s_out) {
+    return serve_run(requests, n_requests, form, hbm_budget_bytes, max_active,
+                     reinterpret_cast<cudaStream_t>(stream), results_out, makespan_s_out);
+}
+
+}  // extern "C"
