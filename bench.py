@@ -1,7 +1,8 @@
 """Benchmark of the GB300 Lloyd k-means engine.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--form auto|plain|mixed-bf16|mixed-fp16] [--workload c3|c2|c1]
+                    [--form auto|plain|mixed-bf16|mixed-fp16]
+                    [--workload c3|c2|c1|c4|c5]
 
 A step is one Lloyd iteration (fused assignment + accumulation, reduction,
 relocation gate, division, shift test) over the whole synthetic data set.
@@ -19,6 +20,19 @@ roofline for the dominant kernel (assignment + accumulation), from its CUDA
          event times inside the timed region.
 cpu_baseline  the CPU oracle (C++/OpenMP restatement of the reference path) on
          a bounded sample of the same workload, scaled to iterations/s.
+serve    p50/p99 request latency and throughput of the serving loop (continuous
+         batching, HBM admission) on the first requests of the c5 stream, for
+         the plain and mixed-fp16 forms (--serve-sample requests; 0 skips it).
+
+--workload c4   256 independent fits (n log-uniform in [2e3, 2e6], d in
+                {8, 16, 32, 64, 128}, k log-uniform in [4, 512], 50 iterations)
+                through the batched engine: instance-iterations/s, beside a
+                loop of single plain fits of the same instances.
+--workload c5   the full serving stream: 10,000 requests, Poisson arrivals at
+                500/s, 80 % fits (n in [1e4, 5e6], d in {16, 32, 64}, k in
+                [8, 1024], tol 1e-4, max_iter 300), 20 % predictions (n in
+                [1e3, 1e6]) against earlier fits, 150 GB admission budget;
+                p50/p99 latency and throughput for the plain and mixed forms.
 
 --impl reference times the reference's algorithm on the host cores.  The
 reference itself (SYCL/DPC++ + dpctl) cannot be built here, so its CPU
@@ -383,6 +397,178 @@ def _roofline(workload, form, n, d, k, kern_ms, clocks, sm_count):
     return r
 
 
+# ---------------------------------------------------------------------------
+# batched fits (c4) and the serving stream (c5)
+# ---------------------------------------------------------------------------
+def _loguniform_int(rng, lo, hi):
+    return int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+
+
+def c4_instances(count=256, seed=4):
+    """(n, d, k, seed) of the c4 batch: n log-U[2e3, 2e6], d in {8..128}, k log-U[4, 512]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = _loguniform_int(rng, 2_000, 2_000_000)
+        d = int(rng.choice([8, 16, 32, 64, 128]))
+        k = min(_loguniform_int(rng, 4, 512), n)
+        out.append((n, d, k, 1000 + i))
+    return out
+
+
+def c5_requests(capi, count=10_000, rate=500.0, seed=5):
+    """The c5 request stream as kmc_serve_request_t records (seeded)."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
+    arr = (capi.ServeRequest * count)()
+    fits = []
+    for r in range(count):
+        if fits and rng.random() < 0.2:
+            m = fits[int(rng.integers(len(fits)))]
+            d, k = arr[m].n_features, arr[m].n_clusters
+            n = _loguniform_int(rng, 1_000, 1_000_000)
+            arr[r] = capi.ServeRequest(float(arrivals[r]), 1, d, n, k, k, 7_000 + r, 0.0, 0, m, 1.0, 1.0)
+        else:
+            n = _loguniform_int(rng, 10_000, 5_000_000)
+            d = int(rng.choice([16, 32, 64]))
+            k = min(_loguniform_int(rng, 8, 1024), n)
+            arr[r] = capi.ServeRequest(float(arrivals[r]), 0, d, n, k, k, 7_000 + r, 1e-4, 300, -1,
+                                       1.0, 1.0)
+            fits.append(r)
+    return arr
+
+
+def serve_stream(L, capi, reqs, count, form, budget=150 * 10 ** 9, max_active=512):
+    """Replays the first `count` requests; returns the latency summary."""
+    import torch
+
+    sub = (capi.ServeRequest * count)(*reqs[:count])
+    res = (capi.ServeResult * count)()
+    mk = ctypes.c_double()
+    capi.check(L.kmc_serve_run(sub, count, FORMS[form], budget, max_active,
+                               torch.cuda.current_stream().cuda_stream, res, ctypes.byref(mk)))
+    lat = np.array([res[r].finish_s - sub[r].arrival_s for r in range(count)])
+    ok = np.array([res[r].status == 0 for r in range(count)])
+    fits = np.array([sub[r].kind == 0 for r in range(count)])
+    return {"requests": count, "completed": int(ok.sum()),
+            "p50_s": float(np.percentile(lat[ok], 50)), "p99_s": float(np.percentile(lat[ok], 99)),
+            "fit_p50_s": float(np.percentile(lat[ok & fits], 50)) if (ok & fits).any() else None,
+            "predict_p50_s": float(np.percentile(lat[ok & ~fits], 50)) if (ok & ~fits).any() else None,
+            "throughput_rps": count / mk.value, "makespan_s": mk.value,
+            "mean_iterations": float(np.mean([res[r].n_iter for r in range(count) if sub[r].kind == 0]))}
+
+
+def run_c5(args, world, rank, local):
+    import torch
+
+    from kmeans_dpcpp_gb300 import capi
+
+    torch.cuda.set_device(local)
+    L = capi.lib()
+    count = args.n or 10_000
+    reqs = c5_requests(capi, count)
+    forms = {}
+    for form in ("mixed-fp16", "plain"):
+        forms[form] = serve_stream(L, capi, reqs, count, form)
+    head = forms["mixed-fp16"]
+    line = {"metric": "serve p50/p99 latency (c5 request stream)", "value": head["p99_s"], "unit": "s",
+            "n_gpus": world, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp16", "data": "synthetic (seeded Gaussian blobs generated on the device at admission)",
+            "config": {"workload": "c5", "requests": count, "arrival_rate_per_s": 500.0,
+                       "hbm_budget_bytes": 150 * 10 ** 9, "parallelism": f"replicas{world}"},
+            "forms": forms}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_c4(args, world, rank, local):
+    import torch
+
+    from kmeans_dpcpp_gb300 import capi
+
+    torch.cuda.set_device(local)
+    L = capi.lib()
+    inst = c4_instances()
+    if args.n:
+        inst = inst[:args.n]
+    stream = torch.cuda.current_stream()
+    s = stream.cuda_stream
+    data = []
+    for (n, d, k, sd) in inst:
+        X = torch.empty((d, n), dtype=torch.float32, device="cuda")
+        capi.check(L.kmc_generate_blobs_f32(X.data_ptr(), n, d, k, -10.0, 10.0, 1.0, 1.0, sd, s))
+        rows = (ctypes.c_int32 * k)()
+        capi.check(L.kmc_seeded_rows(n, k, sd, rows))
+        C0 = X[:, torch.tensor(list(rows), dtype=torch.int64, device="cuda")].contiguous()
+        data.append((X, C0))
+    w_all = {n: torch.ones(n, dtype=torch.float32, device="cuda") for (n, _, _, _) in inst}
+    iters = 50
+    # the autotuner measures each (d, k bucket) once, outside the timed region
+    for (n, d, k, _) in inst:
+        v = ctypes.c_int()
+        capi.check(L.kmc_tile_variant(d, k, s, ctypes.byref(v)))
+
+    def batched():
+        h = ctypes.c_void_p()
+        capi.check(L.kmc_batch_create(len(inst), s, ctypes.byref(h)))
+        keep = []
+        try:
+            for (n, d, k, _), (X, C0) in zip(inst, data):
+                C = C0.clone()
+                lab = torch.empty(n, dtype=torch.int32, device="cuda")
+                keep.append((C, lab))
+                q = ctypes.c_int64()
+                capi.check(L.kmc_batch_add_fit_f32(h, X.data_ptr(), w_all[n].data_ptr(), C.data_ptr(),
+                                                   lab.data_ptr(), n, d, k, 0.0, iters, ctypes.byref(q)))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            capi.check(L.kmc_batch_run(h))
+            torch.cuda.synchronize()
+            return time.perf_counter() - t0
+        finally:
+            capi.check(L.kmc_batch_destroy(h))
+
+    def single_loop():
+        t = 0.0
+        for (n, d, k, _), (X, C0) in zip(inst, data):
+            C = C0.clone()
+            res = torch.empty_like(C)
+            lab = torch.empty(n, dtype=torch.int32, device="cuda")
+            fit = ctypes.c_void_p()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            capi.check(L.kmc_fit_create_f32_i32(X.data_ptr(), w_all[n].data_ptr(), C.data_ptr(),
+                                                lab.data_ptr(), res.data_ptr(), n, d, k, 0.0, iters, 0, s,
+                                                ctypes.byref(fit)))
+            try:
+                capi.check(L.kmc_fit_run(fit))
+                it, inr = ctypes.c_int64(), ctypes.c_double()
+                capi.check(L.kmc_fit_finalize(fit, ctypes.byref(it), ctypes.byref(inr)))
+            finally:
+                capi.check(L.kmc_fit_destroy(fit))
+            torch.cuda.synchronize()
+            t += time.perf_counter() - t0
+        return t
+
+    batched()  # warm-up: allocator pools, graphs, kernel attributes
+    t_batch = batched()
+    t_single = single_loop()
+    total = len(inst) * iters
+    flops = sum(2.0 * n * k * d for (n, d, k, _) in inst) * iters
+    line = {"metric": "batched fits: instance-iterations/s (c4)", "value": total / t_batch,
+            "unit": "instance-iter/s", "n_gpus": world, "steps": iters, "warmup": 1,
+            "ms_per_step": 1e3 * t_batch / iters, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian blobs on the device)",
+            "config": {"workload": "c4", "instances": len(inst), "iterations": iters,
+                       "total_samples": sum(i[0] for i in inst), "parallelism": f"replicas{world}"},
+            "distance_tflops": flops / t_batch / 1e12,
+            "single_fit_loop": {"value": total / t_single, "seconds": t_single},
+            "speedup_vs_single_fit_loop": t_single / t_batch,
+            "batched_seconds": t_batch}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_gb300(args, world, rank, local):
     import torch
 
@@ -462,6 +648,12 @@ def run_gb300(args, world, rank, local):
     }
     if "plain" in forms and form != "plain":
         line["speedup_vs_plain_fp32"] = head["value"] / forms["plain"]["value"]
+    if args.serve_sample > 0:
+        reqs = c5_requests(capi, args.serve_sample)
+        line["serve"] = {"sample": "first %d requests of the c5 stream (Poisson 500/s, 150 GB "
+                                   "admission budget)" % args.serve_sample,
+                         "forms": {f: serve_stream(L, capi, reqs, args.serve_sample, f)
+                                   for f in ("mixed-fp16", "plain")}}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(X_t, C0, target_s=args.cpu_seconds)
     if rank == 0:
@@ -475,14 +667,17 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--form", choices=["auto"] + sorted(FORMS), default="auto")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c3")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["c4", "c5"], default="c3")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true",
                     help="time only the headline form (no plain / other mixed comparison)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--n", type=int, default=None,
-                    help="fewer samples than the workload names (small profiling captures)")
+                    help="fewer samples than the workload names (small profiling captures); "
+                         "for c4 / c5 the number of instances / requests")
+    ap.add_argument("--serve-sample", type=int, default=300,
+                    help="requests of the c5 stream replayed for the serve key (0: skip)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
@@ -492,7 +687,12 @@ def main(argv=None):
         run_reference(args, world, rank)
         return
     world, rank, local = dist_setup(args.gpus)
-    run_gb300(args, world, rank, local)
+    if args.workload == "c4":
+        run_c4(args, world, rank, local)
+    elif args.workload == "c5":
+        run_c5(args, world, rank, local)
+    else:
+        run_gb300(args, world, rank, local)
     if world > 1:
         import torch.distributed as dist
 
