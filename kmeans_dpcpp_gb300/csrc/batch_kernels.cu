@@ -12,7 +12,7 @@
 //                 (src/device_functions.hpp:106-162) -- so labels equal a
 //                 single fit's bit for bit.  Fitting instances add w*x into
 //                 float64 sums, privatised per item in shared memory when the
-//                 instance's k*(d+1) doubles fit in 48 KB.  Three kernels
+//                 instance's k*(d+1) doubles fit in 72 KB.  Three kernels
 //                 differ in the centroid window (32, 64 or 128 columns per
 //                 pass); the autotuner picks one per (d, k)
 //   batch_reduce  one CTA per fitting instance: sums rounded once to float32,
@@ -39,7 +39,7 @@ namespace {
 constexpr int kThreadsB = 256;
 constexpr int kBK = 16;
 constexpr int kTM = 8;
-constexpr size_t kPrivBytes = 48 * 1024;
+constexpr size_t kPrivBytes = 72 * 1024;  // with the tiles: two CTAs per SM
 
 // Deterministic block-wide float64 sum (same shape as the single-fit loop
 // control: warp shuffles, then warp 0 over the warp totals).

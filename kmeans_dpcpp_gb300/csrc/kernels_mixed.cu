@@ -213,12 +213,6 @@ __device__ __forceinline__ bool epi_any(bool v) {
     return r != 0;
 }
 
-// Position of the n-th (0-based) set bit of m (m has more than n set bits).
-__device__ __forceinline__ int nth_set_bit(uint32_t m, int n) {
-    for (int q = 0; q < n; ++q) m &= m - 1u;
-    return __ffs(m) - 1;
-}
-
 template <int BF16>
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
     if (BF16) {
@@ -841,101 +835,87 @@ __global__ void bound_kernel(const float *cn2, const float *cn1, const float *hn
 }
 
 // Exact fp32 re-evaluation of samples whose margin did not certify them: the
-// reference's arithmetic (sequential fma dot, hn - dot, strict < in
-// ascending centroid order) over the candidate set, one warp per sample.  The
-// sample's features come from the row-major fp32 copy of X and the centroids
-// from their transposed fp32 copy (one contiguous row each).
-__global__ void recheck_kernel(const float *xrow, const float *ct, const float *hn,
-                               const float *w, const uint4 *cand, const int *flagged,
-                               const int *n_flagged, int64_t n, int64_t d, int64_t k, int64_t d4,
-                               void *labels, int label64, int update, int acc_f64, float *sums32,
-                               double *acc64, int64_t k_pad, int n_copies,
-                               const LoopState *guard) {
+// reference's arithmetic (sequential fma dot over f = 0..d-1, hn - dot,
+// strict < with the lowest index on ties) over the candidate set (hot
+// sub-chunks x hot classes of each column half), one thread per sample so
+// that thousands of samples are in flight.  The sample's features come from
+// the row-major fp32 copy of X (cached in L1 across its candidates) and the
+// centroids from their transposed fp32 copy (one contiguous row each).
+__global__ void __launch_bounds__(256) recheck_kernel(
+    const float *xrow, const float *ct, const float *hn, const float *w, const uint4 *cand,
+    const int *flagged, const int *n_flagged, int64_t n, int64_t d, int64_t k, int64_t d4,
+    void *labels, int label64, int update, int acc_f64, float *sums32, double *acc64,
+    int64_t k_pad, int n_copies, const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
-    extern __shared__ __align__(16) float xs[];  // [warps][d4]
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     {
         // this block's share of the per-CTA copies of the cluster sums
         const int64_t copy = (int64_t)(blockIdx.x % (unsigned)n_copies) * (k_pad * d4 + k_pad);
         sums32 += copy;
         acc64 += copy;
     }
-    float *x = xs + (size_t)wib * d4;
     const int64_t nf = (int64_t)*n_flagged;
     const int64_t total = nf < n ? nf : n;
-    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t e = blockIdx.x * (int64_t)(blockDim.x >> 5) + wib; e < total; e += nwarps) {
+    const int64_t g4 = d4 / 4;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = flagged[e];
         if (i < 0 || i >= n) continue;
-        for (int64_t f = lane; f < d4; f += 32) x[f] = xrow[i * d4 + f];
-        __syncwarp();
+        const float4 *xr = reinterpret_cast<const float4 *>(xrow + i * d4);
         const uint4 cm = cand[i];
-        const uint32_t h1[2] = {cm.x, cm.y}, h2[2] = {cm.z, cm.w};
-        // candidate columns (sub-chunk x class) of both halves; lane L takes
-        // candidates L, L + 32, ...
-        const int n2[2] = {__popc(h2[0]), __popc(h2[1])};
-        const int ncand = __popc(h1[0]) * n2[0] + __popc(h1[1]) * n2[1];
         float best = pos_inf<float>();
         int bj = 0;
-        for (int q = lane; q < ncand; q += 32) {
-            int r = q, h = 0;
-            if (r >= __popc(h1[0]) * n2[0]) {
-                r -= __popc(h1[0]) * n2[0];
-                h = 1;
-            }
-            const int si = r / n2[h], ti = r % n2[h];
-            const int s = nth_set_bit(h1[h], si);
-            const int t = nth_set_bit(h2[h], ti);
-            const int64_t j = (int64_t)(s >> 2) * kChunkN + h * 128 + (s & 3) * 32 + t;
-            if (j >= k) continue;
-            const float4 *cr = reinterpret_cast<const float4 *>(ct + j * d4);
-            const float4 *xr = reinterpret_cast<const float4 *>(x);
-            float dot = 0.f;
-            for (int64_t g = 0; g < d4 / 4; ++g) {
-                const float4 cv = __ldg(cr + g);
-                const float4 xv = xr[g];
-                dot = __fmaf_rn(xv.x, cv.x, dot);
-                if (4 * g + 1 < d) dot = __fmaf_rn(xv.y, cv.y, dot);
-                if (4 * g + 2 < d) dot = __fmaf_rn(xv.z, cv.z, dot);
-                if (4 * g + 3 < d) dot = __fmaf_rn(xv.w, cv.w, dot);
-            }
-            const float D = hn[j] - dot;
-            if (D < best || (D == best && j < bj)) {
-                best = D;
-                bj = (int)j;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t m1 = h ? cm.y : cm.x, m2 = h ? cm.w : cm.z;
+            for (uint32_t a1 = m1; a1 != 0u; a1 &= a1 - 1u) {
+                const int sc = __ffs(a1) - 1;
+                for (uint32_t a2 = m2; a2 != 0u; a2 &= a2 - 1u) {
+                    const int t = __ffs(a2) - 1;
+                    const int64_t j = (int64_t)(sc >> 2) * kChunkN + h * 128 + (sc & 3) * 32 + t;
+                    if (j >= k) continue;
+                    const float4 *cr = reinterpret_cast<const float4 *>(ct + j * d4);
+                    float dot = 0.f;
+                    for (int64_t g = 0; g < g4; ++g) {
+                        const float4 xv = __ldg(xr + g), cv = __ldg(cr + g);
+                        dot = __fmaf_rn(xv.x, cv.x, dot);
+                        if (4 * g + 1 < d) dot = __fmaf_rn(xv.y, cv.y, dot);
+                        if (4 * g + 2 < d) dot = __fmaf_rn(xv.z, cv.z, dot);
+                        if (4 * g + 3 < d) dot = __fmaf_rn(xv.w, cv.w, dot);
+                    }
+                    const float D = hn[j] - dot;
+                    if (D < best || (D == best && j < bj)) {
+                        best = D;
+                        bj = (int)j;
+                    }
+                }
             }
         }
-        for (int off = 16; off > 0; off >>= 1) {
-            const float ob = __shfl_xor_sync(0xffffffffu, best, off);
-            const int oj = __shfl_xor_sync(0xffffffffu, bj, off);
-            if (ob < best || (ob == best && oj < bj)) {
-                best = ob;
-                bj = oj;
-            }
-        }
-        if (lane == 0) {
-            if (label64)
-                reinterpret_cast<int64_t *>(labels)[i] = bj;
-            else
-                reinterpret_cast<int32_t *>(labels)[i] = bj;
-        }
+        if (label64)
+            reinterpret_cast<int64_t *>(labels)[i] = bj;
+        else
+            reinterpret_cast<int32_t *>(labels)[i] = bj;
         if (update) {
             const float wv = w[i];
-            for (int64_t f = lane; f < d; f += 32) {
-                const float v = __fmul_rn(x[f], wv);
-                if (acc_f64)
-                    atomicAdd(acc64 + (int64_t)bj * d4 + f, (double)v);
-                else
-                    atomicAdd(sums32 + (int64_t)bj * d4 + f, v);
-            }
-            if (lane == 0) {
-                if (acc_f64)
-                    atomicAdd(acc64 + k_pad * d4 + bj, (double)wv);
-                else
-                    atomicAdd(sums32 + k_pad * d4 + bj, wv);
+            if (acc_f64) {
+                double *dst = acc64 + (int64_t)bj * d4;
+                for (int64_t g = 0; g < g4; ++g) {
+                    const float4 xv = __ldg(xr + g);
+                    atomicAdd(dst + 4 * g + 0, (double)__fmul_rn(xv.x, wv));
+                    atomicAdd(dst + 4 * g + 1, (double)__fmul_rn(xv.y, wv));
+                    atomicAdd(dst + 4 * g + 2, (double)__fmul_rn(xv.z, wv));
+                    atomicAdd(dst + 4 * g + 3, (double)__fmul_rn(xv.w, wv));
+                }
+                atomicAdd(acc64 + k_pad * d4 + bj, (double)wv);
+            } else {
+                float4 *dst = reinterpret_cast<float4 *>(sums32 + (int64_t)bj * d4);
+                for (int64_t g = 0; g < g4; ++g) {
+                    const float4 xv = __ldg(xr + g);
+                    atomicAdd(dst + g, make_float4(__fmul_rn(xv.x, wv), __fmul_rn(xv.y, wv),
+                                                   __fmul_rn(xv.z, wv), __fmul_rn(xv.w, wv)));
+                }
+                atomicAdd(sums32 + k_pad * d4 + bj, wv);
             }
         }
-        __syncwarp();
     }
 }
 
@@ -1195,9 +1175,7 @@ struct MixedFit : PlainFit<float, I> {
             kern<<<(unsigned)grid, kThreadsMixed, L.total, s>>>(a);
             KMC_TRY(check_launch("mixed_assign"));
         }
-        const int rblock = 256;
-        const size_t rsmem = sizeof(float) * (rblock / 32) * d4;
-        recheck_kernel<<<(unsigned)(num_sms() * 4), rblock, rsmem, s>>>(
+        recheck_kernel<<<(unsigned)(num_sms() * 8), 256, 0, s>>>(
             xrow, ct, this->hn, p.w, cand, flagged, n_flagged, p.n, p.d, p.k, d4, p.labels,
             a.label64, update, acc_f64, sums32, acc64, k_pad, n_copies, guard);
         KMC_TRY(check_launch("mixed_recheck"));

@@ -98,6 +98,10 @@ struct BatchEngine {
     cudaStream_t user = nullptr;
     cudaStream_t s = nullptr;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    // the assign variants run as parallel branches of graph A, so each one's
+    // tail overlaps the others instead of leaving SMs idle
+    cudaStream_t side[kBatchVariants] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr, ev_join[kBatchVariants] = {nullptr, nullptr, nullptr};
     int64_t cap = 0;
     Scratch dev;                    // table, lists, work queue, counters, status
     BInst *tab_d = nullptr;
@@ -135,6 +139,11 @@ struct BatchEngine {
         }
         if (ev_in) cudaEventDestroy(ev_in);
         if (ev_out) cudaEventDestroy(ev_out);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        for (int v = 0; v < kBatchVariants; ++v) {
+            if (side[v]) cudaStreamDestroy(side[v]);
+            if (ev_join[v]) cudaEventDestroy(ev_join[v]);
+        }
     }
 
     int init(int64_t capacity, cudaStream_t stream) {
@@ -143,6 +152,11 @@ struct BatchEngine {
         KMC_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
         KMC_CUDA_TRY(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
         KMC_CUDA_TRY(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
+        KMC_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+        for (int v = 0; v < kBatchVariants; ++v) {
+            KMC_CUDA_TRY(cudaStreamCreateWithFlags(&side[v], cudaStreamNonBlocking));
+            KMC_CUDA_TRY(cudaEventCreateWithFlags(&ev_join[v], cudaEventDisableTiming));
+        }
         cap = capacity;
         const size_t o_tab = 0;
         const size_t o_all = o_tab + align256(sizeof(BInst) * cap);
@@ -292,9 +306,15 @@ struct BatchEngine {
         KMC_TRY(prepare_batch_assign());
         KMC_TRY(capture(&gA, [&]() -> int {
             KMC_TRY(launch_batch_prep(tab_d, all_d, (int)all.size(), counters_d, s));
-            for (int v = 0; v < kBatchVariants; ++v)
+            KMC_CUDA_TRY(cudaEventRecord(ev_fork, s));
+            for (int v = 0; v < kBatchVariants; ++v) {
+                if (n_items[v] == 0) continue;
+                KMC_CUDA_TRY(cudaStreamWaitEvent(side[v], ev_fork, 0));
                 KMC_TRY(launch_batch_assign(v, tab_d, items_d + item_off[v], n_items[v],
-                                            counters_d + v, s));
+                                            counters_d + v, side[v]));
+                KMC_CUDA_TRY(cudaEventRecord(ev_join[v], side[v]));
+                KMC_CUDA_TRY(cudaStreamWaitEvent(s, ev_join[v], 0));
+            }
             return launch_batch_reduce(tab_d, fit_d, (int)fits.size(), nempty_d, s);
         }));
         KMC_TRY(capture(&gB, [&]() -> int {
