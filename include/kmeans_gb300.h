@@ -442,6 +442,38 @@ int kmc_fit_rechecked(kmc_fit_t fit, int64_t *last_out, int64_t *total_out, int 
 int kmc_fit_launch_count(kmc_fit_t fit, int64_t *launches_out);
 int kmc_fit_destroy(kmc_fit_t fit);
 
+/* ---- input layout and initialisation -----------------------------------------------
+ * No counterpart in the reference, which takes the feature-major X_t and the
+ * initial centroids as given (_kmeans_lloyd.cpp:1153); these are the steps
+ * before its path.  kmc_transpose_* turns row-major X (n_samples, n_features)
+ * into X_t (n_features, n_samples).  kmc_gather_rows_* copies the given rows
+ * of X_t into centroids_t (random-row initialisation; rows in [0, n)).
+ * kmc_kmeans_plusplus_* seeds k centroids by D^2 sampling on the device,
+ * deterministic for a seed (sample_weight may be NULL); chosen_rows receives
+ * the k sample indices. */
+int kmc_transpose_f32(const float *X, float *X_t, int64_t n_samples, int64_t n_features,
+                      kmc_stream_t stream);
+int kmc_transpose_f64(const double *X, double *X_t, int64_t n_samples, int64_t n_features,
+                      kmc_stream_t stream);
+int kmc_gather_rows_f32(const float *X_t, int64_t n_samples, int64_t n_features,
+                        const int32_t *rows, int64_t n_clusters, float *centroids_t,
+                        kmc_stream_t stream);
+int kmc_gather_rows_f64(const double *X_t, int64_t n_samples, int64_t n_features,
+                        const int32_t *rows, int64_t n_clusters, double *centroids_t,
+                        kmc_stream_t stream);
+/* Mean over features of each feature's population variance (float64; the
+ * scale scikit-learn's Lloyd engine applies to tol). */
+int kmc_mean_feature_variance_f32(const float *X_t, int64_t n_samples, int64_t n_features,
+                                  double *mean_variance_out, kmc_stream_t stream);
+int kmc_mean_feature_variance_f64(const double *X_t, int64_t n_samples, int64_t n_features,
+                                  double *mean_variance_out, kmc_stream_t stream);
+int kmc_kmeans_plusplus_f32(const float *X_t, const float *sample_weight, int64_t n_samples,
+                            int64_t n_features, int64_t n_clusters, uint64_t seed,
+                            float *centroids_t, int32_t *chosen_rows, kmc_stream_t stream);
+int kmc_kmeans_plusplus_f64(const double *X_t, const double *sample_weight, int64_t n_samples,
+                            int64_t n_features, int64_t n_clusters, uint64_t seed,
+                            double *centroids_t, int32_t *chosen_rows, kmc_stream_t stream);
+
 /* ---- batched fits ------------------------------------------------------------------
  * No counterpart in the reference (the benchmark spec's batching and serving
  * row).  Many independent float32 fits and label-only predictions of uneven

@@ -50,6 +50,10 @@ __all__ = [
     "kmeans_lloyd_driver",
 ]
 
+# scikit-learn-style estimator over the module (not part of the reference's
+# surface, so it stays out of __all__)
+from .estimator import KMeans  # noqa: E402,F401
+
 __doc__ += """
 This module implements GB300 offloading routines necessary for implementing
 Lloyd's algorithm to solve the K-Means problem.

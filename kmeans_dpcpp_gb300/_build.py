@@ -45,6 +45,7 @@ CU_SOURCES = [
     "noalloc.cu",
     "batch_kernels.cu",
     "serve.cu",
+    "init.cu",
 ]
 HEADERS = ["km_common.cuh", "km_kernels.cuh", "km_fit.cuh", "km_mixed.cuh", "km_batch.cuh"]
 

@@ -331,6 +331,74 @@ int64_t driver(const T *X, const T *w, T *init_c, I *labels, T *res_c, int64_t n
     return it;
 }
 
+// k-means++ seeding as the engine's kmc_kmeans_plusplus_* defines it (not a
+// reference function: the reference takes initial centroids as given).  Draw
+// u_t = SplitMix64(seed ^ SplitMix64(t)) >> 11 scaled to [0, 1); values v_i =
+// w_i (t = 0) or w_i * min_j ||x_i - c_j||^2 (float64 products of the dataT
+// distance); float64 sums run sequentially inside blocks of 4096 samples and
+// then over the blocks; the pick is the first i whose running sum exceeds
+// u_t * total (or the block's last positive sample if rounding overshoots).
+uint64_t splitmix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+template <typename T>
+void kmeanspp(const T *X, const T *w, int64_t n, int64_t d, int64_t k, uint64_t seed, T *C,
+              int32_t *chosen) {
+    const int64_t B = 4096, nb = (n + B - 1) / B;
+    std::vector<T> md(n, T(0));
+    std::vector<double> part(nb);
+    for (int64_t t = 0; t < k; ++t) {
+        const bool use_d2 = t > 0;
+        auto val = [&](int64_t i) {
+            const double wi = w ? (double)w[i] : 1.0;
+            return use_d2 ? wi * (double)md[i] : wi;
+        };
+        for (int64_t b = 0; b < nb; ++b) {
+            double s = 0.0;
+            for (int64_t i = b * B; i < std::min(n, (b + 1) * B); ++i) s += val(i);
+            part[b] = s;
+        }
+        double total = 0.0;
+        for (int64_t b = 0; b < nb; ++b) total += part[b];
+        int64_t sel = -1;
+        if (total > 0.0) {
+            const double u = (double)(splitmix64(seed ^ splitmix64((uint64_t)t)) >> 11) * 0x1p-53;
+            const double target = u * total;
+            double run = 0.0;
+            int64_t b = 0;
+            for (; b < nb; ++b) {
+                if (run + part[b] > target) break;
+                run += part[b];
+            }
+            if (b == nb) b = nb - 1;
+            for (int64_t i = b * B; i < std::min(n, (b + 1) * B); ++i) {
+                const double v = val(i);
+                if (v > 0.0) sel = i;
+                run += v;
+                if (run > target && v > 0.0) break;
+            }
+        }
+        if (sel < 0) sel = t > 0 ? ((int64_t)chosen[t - 1] + 1) % n : 0;
+        chosen[t] = (int32_t)sel;
+        for (int64_t f = 0; f < d; ++f) C[f * k + t] = X[f * n + sel];
+        if (t + 1 < k) {
+#pragma omp parallel for schedule(static)
+            for (int64_t i = 0; i < n; ++i) {
+                T acc = T(0);
+                for (int64_t f = 0; f < d; ++f) {
+                    const T diff = X[f * n + i] - X[f * n + sel];
+                    acc = fma_t(diff, diff, acc);
+                }
+                md[i] = (t == 0 || acc < md[i]) ? acc : md[i];
+            }
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -403,5 +471,14 @@ void kmref_set_num_threads(int t) {
 
 KMREF_T(f32, float)
 KMREF_T(f64, double)
+
+void kmref_kmeanspp_f32(const float *X, const float *w, int64_t n, int64_t d, int64_t k,
+                        uint64_t seed, float *C, int32_t *chosen) {
+    kmeanspp<float>(X, w, n, d, k, seed, C, chosen);
+}
+void kmref_kmeanspp_f64(const double *X, const double *w, int64_t n, int64_t d, int64_t k,
+                        uint64_t seed, double *C, int32_t *chosen) {
+    kmeanspp<double>(X, w, n, d, k, seed, C, chosen);
+}
 
 }  // extern "C"

@@ -55,6 +55,9 @@ def lib():
             f = getattr(L, f"kmref_driver_{suf}")
             f.argtypes = [_p] * 5 + [_c_i64] * 3 + [_c_dbl, _c_i64, _p, _p]
             f.restype = _c_i64
+        for suf in ("f32", "f64"):
+            getattr(L, f"kmref_kmeanspp_{suf}").argtypes = [_p, _p, _c_i64, _c_i64, _c_i64,
+                                                             ctypes.c_uint64, _p, _p]
         L.kmref_num_threads.restype = ctypes.c_int
         L.kmref_set_num_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -215,3 +218,14 @@ def kmeans_lloyd_driver(X_t, w, init_C, tol, max_iter):
         _ptr(X_t), _ptr(w), _ptr(C), _ptr(lab), _ptr(res), n, d, k, float(tol), int(max_iter),
         _ptr(inr), _ptr(rel))
     return int(it), lab, res, float(inr[0]), int(rel[0])
+
+
+def kmeans_plusplus(X_t, k, seed, w=None):
+    """k-means++ rows and centroids (d, k), the engine's seeding restated."""
+    X_t = _c(X_t)
+    w = None if w is None else _c(w, X_t.dtype)
+    d, n = X_t.shape
+    C = np.empty((d, k), X_t.dtype)
+    rows = np.empty(k, np.int32)
+    getattr(lib(), f"kmref_kmeanspp_{_suf(X_t.dtype)}")(_ptr(X_t), _ptr(w), n, d, k, seed, _ptr(C), _ptr(rows))
+    return rows, C
