@@ -199,16 +199,18 @@ __device__ __forceinline__ void mask_tail(uint32_t (&r)[32], int64_t j0, int64_t
     }
 }
 
-__device__ __forceinline__ bool epi_any(bool v) {
-    // OR over the 256 epilogue threads (named barrier 1)
+// OR over the 64 epilogue threads of TMEM lane quadrant q (the two warps that
+// scan the two column halves of the same rows), named barrier 8 + q.  Only
+// these two warps exchange data, so the other quadrants are not held back.
+__device__ __forceinline__ bool pair_any(bool v, int q) {
     uint32_t r;
     asm volatile(
         "{\n\t.reg .pred p, q;\n\t"
         "setp.ne.u32 p, %1, 0;\n\t"
-        "barrier.red.or.pred q, 1, 256, p;\n\t"
+        "barrier.red.or.pred q, %2, 64, p;\n\t"
         "selp.u32 %0, 1, 0, q;\n\t}"
         : "=r"(r)
-        : "r"((uint32_t)v)
+        : "r"((uint32_t)v), "r"(8 + q)
         : "memory");
     return r != 0;
 }
@@ -472,8 +474,8 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
             // best score of this half, exchanged with the other half
             float *xb = xch + (size_t)(tl & 1) * (2 * kTileM);
             xb[h * kTileM + row] = Mh;
-            // one barrier per tile: publishes the exchange and agrees on errors
-            if (epi_any(bad || *err != 0)) break;
+            // one pair barrier per tile: publishes the exchange and agrees on errors
+            if (pair_any(bad || *err != 0, q)) break;
             const float Mo = xb[(h ^ 1) * kTileM + row];
             // Columns whose score reaches thr = M - E2 can hold the reference's
             // winner (every score is within E2 / 2 of its exact value).  The
@@ -875,6 +877,9 @@ __global__ void __launch_bounds__(256) recheck_kernel(
                     if (j >= k) continue;
                     const float4 *cr = reinterpret_cast<const float4 *>(ct + j * d4);
                     float dot = 0.f;
+                    // unrolled so that a candidate's row loads are in flight
+                    // before its fma chain needs them
+#pragma unroll 8
                     for (int64_t g = 0; g < g4; ++g) {
                         const float4 xv = __ldg(xr + g), cv = __ldg(cr + g);
                         dot = __fmaf_rn(xv.x, cv.x, dot);
