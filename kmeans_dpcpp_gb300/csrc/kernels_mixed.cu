@@ -663,7 +663,7 @@ __global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int64_t d4,
          i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t tile = i / kTileM;
         const uint32_t r = (uint32_t)(i % kTileM);
-        double s2 = 0.0, s1 = 0.0;
+        float s2 = 0.f, s1 = 0.f;  // float32 sums, bounded from above below
         for (int kb = 0; kb < nkb; ++kb) {
             uint8_t *base = img + ((size_t)tile * nkb + kb) * kTileBytes;
             for (int ch = 0; ch < 8; ++ch) {
@@ -672,8 +672,8 @@ __global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int64_t d4,
                 for (int e = 0; e < 8; ++e) {
                     const int64_t f = (int64_t)kb * 64 + ch * 8 + e;
                     const float x = (i < n && f < d) ? X[f * n + i] : 0.f;
-                    s2 += (double)x * (double)x;
-                    s1 += fabs((double)x);
+                    s2 = __fmaf_rn(x, x, s2);
+                    s1 = __fadd_rn(s1, fabsf(x));
                     v[e] = x * sigma;
                     xr[e] = x;
                 }
@@ -692,8 +692,13 @@ __global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int64_t d4,
             }
         }
         if (i < n) {
-            nx[i] = __double2float_ru(sqrt(s2) * (1.0 + 1e-12));
-            n1[i] = __double2float_ru(s1 * (1.0 + 1e-12));
+            // A float32 sum of m non-negative terms (each rounded once) is at
+            // least (1 - 2^-24)^m times the exact sum; m <= 128 here, so the
+            // factor 1 + (m + 2) 2^-23 applied with upward rounding (and an
+            // upward square root) gives upper bounds of ||x||_2 and ||x||_1.
+            const float grow = 1.f + (float)(nkb * 64 + 2) * 0x1p-23f;
+            nx[i] = __fsqrt_ru(__fmul_ru(s2, grow));
+            n1[i] = __fmul_ru(s1, grow);
         }
     }
 }
