@@ -31,6 +31,10 @@ int PlainFit<T, I>::init(const FitParams<T, I> &p) {
     prm = p;
     const int64_t n = p.n, d = p.d, k = p.k;
     KMC_CHECK_ARG(n >= 0 && d >= 0 && k >= 0, "negative array dimension");
+    // Small sums get one float64 copy per CTA of the fused step (two CTAs
+    // per SM), filled with fire-and-forget global reductions; shared-memory
+    // float64 atomics would be compare-and-swap loops on the critical path.
+    P = ((d + 1) * k <= 8192) ? 2 * (int64_t)num_sms() : 1;
     size_t off = 0;
     auto take = [&](size_t bytes) {
         size_t o = off;

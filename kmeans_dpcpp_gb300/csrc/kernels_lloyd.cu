@@ -18,7 +18,10 @@
 // argmin of each sample is reduced across the 16 threads that share it with
 // warp shuffles.  Centroid sums are privatised per CTA in shared memory when
 // (d + 1) * k fits, and flushed once per CTA with atomics; otherwise they go
-// straight to the global private copy with atomics.
+// straight to the global private copy with atomics.  float64 sums with one
+// global copy per CTA always take the global route: float64 reductions to
+// global memory are native (fire-and-forget), in shared memory they are
+// compare-and-swap loops.
 #include "km_kernels.cuh"
 
 namespace kmc {
@@ -119,6 +122,39 @@ __global__ void __launch_bounds__(kThreads, 2) tile_kernel(TileArgs<T, I, A> a) 
     const int64_t num_tiles = ceil_div<int64_t>(n, BM);
     const int nchunks = (int)ceil_div<int64_t>(d, BK);
 
+    // Feature chunk ch of the samples i0.. and centroids c0.. into registers.
+    // The CTA's (tile, centroid tile) steps run in order, and chunk 0 of the
+    // next step is loaded while the last chunk of the current one is
+    // multiplied, so global-memory latency is not paid at step boundaries
+    // (the assignment-only mode loads it at the step itself: it has no
+    // registers to spare across its epilogue).
+    constexpr bool kAhead = MODE != MODE_ASSIGN;
+    T xr[XR], cr[CR];
+    auto load_regs = [&](int64_t li0, int64_t lc0, int ch) {
+        const int64_t f0 = (int64_t)ch * BK;
+#pragma unroll
+        for (int r = 0; r < XR; ++r) {
+            int e = tid + r * kThreads;
+            int kk = e / BM, s = e % BM;
+            int64_t f = f0 + kk, i = li0 + s;
+            xr[r] = (f < d && i < n) ? a.X[f * n + i] : T(0);
+        }
+#pragma unroll
+        for (int r = 0; r < CR; ++r) {
+            int e = tid + r * kThreads;
+            int kk = e / BN, c = e % BN;
+            int64_t f = f0 + kk, j = lc0 + c;
+            cr[r] = (f < d && j < k) ? a.C[f * k + j] : T(0);
+        }
+    };
+    auto store_smem = [&](int buf) {
+#pragma unroll
+        for (int r = 0; r < XR; ++r) Xs[buf * BK * BM + tid + r * kThreads] = xr[r];
+#pragma unroll
+        for (int r = 0; r < CR; ++r) Cs[buf * BK * BN + tid + r * kThreads] = cr[r];
+    };
+    if (kAhead && (int64_t)blockIdx.x < num_tiles) load_regs((int64_t)blockIdx.x * BM, 0, 0);
+
     for (int64_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
         const int64_t i0 = tile * BM;
         T best[TM];
@@ -141,37 +177,18 @@ __global__ void __launch_bounds__(kThreads, 2) tile_kernel(TileArgs<T, I, A> a) 
                     hs[c] = (c0 + c < k) ? a.hn[c0 + c] : pos_inf<T>();
             }
 
-            T xr[XR], cr[CR];
-            auto load_regs = [&](int ch) {
-                const int64_t f0 = (int64_t)ch * BK;
-#pragma unroll
-                for (int r = 0; r < XR; ++r) {
-                    int e = tid + r * kThreads;
-                    int kk = e / BM, s = e % BM;
-                    int64_t f = f0 + kk, i = i0 + s;
-                    xr[r] = (f < d && i < n) ? a.X[f * n + i] : T(0);
-                }
-#pragma unroll
-                for (int r = 0; r < CR; ++r) {
-                    int e = tid + r * kThreads;
-                    int kk = e / BN, c = e % BN;
-                    int64_t f = f0 + kk, j = c0 + c;
-                    cr[r] = (f < d && j < k) ? a.C[f * k + j] : T(0);
-                }
-            };
-            auto store_smem = [&](int buf) {
-#pragma unroll
-                for (int r = 0; r < XR; ++r) Xs[buf * BK * BM + tid + r * kThreads] = xr[r];
-#pragma unroll
-                for (int r = 0; r < CR; ++r) Cs[buf * BK * BN + tid + r * kThreads] = cr[r];
-            };
-
-            load_regs(0);
-            store_smem(0);
+            if (!kAhead) load_regs(i0, c0, 0);
+            store_smem(0);  // chunk 0 (loaded during the previous step when kAhead)
             __syncthreads();
             for (int ch = 0; ch < nchunks; ++ch) {
                 const int buf = ch & 1;
-                if (ch + 1 < nchunks) load_regs(ch + 1);
+                if (ch + 1 < nchunks) {
+                    load_regs(i0, c0, ch + 1);
+                } else if (kAhead && c0 + BN < k) {
+                    load_regs(i0, c0 + BN, 0);
+                } else if (kAhead && tile + gridDim.x < num_tiles) {
+                    load_regs((tile + gridDim.x) * BM, 0, 0);
+                }
                 const T *xb = Xs + buf * BK * BM;
                 const T *cb = Cs + buf * BK * BN;
 #pragma unroll
@@ -271,7 +288,10 @@ __global__ void __launch_bounds__(kThreads, 2) tile_kernel(TileArgs<T, I, A> a) 
                 int64_t f = e / BM;
                 int64_t i = i0 + s;
                 if (i < n) {
-                    T val = mul_rn(a.X[f * n + i], ws[s]);
+                    // up to BK features the tile's samples are still in chunk
+                    // buffer 0 of shared memory
+                    const T xv = (nchunks == 1) ? Xs[f * BM + s] : a.X[f * n + i];
+                    T val = mul_rn(xv, ws[s]);
                     atomicAdd(&tsums[f * k + labs[s]], (A)val);
                 }
             }
@@ -331,7 +351,11 @@ template <typename T, typename I, typename A>
 int launch_fused_step(const T *X, const T *w, const T *C, const T *hn, I *labels, A *sums_cp,
                       A *sizes_cp, int64_t n, int64_t d, int64_t k, int64_t P, cudaStream_t s,
                       const LoopState *guard) {
-    int priv = (sizeof(A) * (size_t)(d * k + k) <= kPrivMaxBytes) ? 1 : 0;
+    // float64 sums with one copy per CTA go straight to global memory
+    // (native reductions); otherwise small sums are privatised in shared memory
+    int priv = (sizeof(A) * (size_t)(d * k + k) <= kPrivMaxBytes && !(sizeof(A) == 8 && P > 1))
+                   ? 1
+                   : 0;
     TileArgs<T, I, A> a{X, w, C, hn, labels, sums_cp, sizes_cp, nullptr, n, d, k, P, priv, guard};
     return launch_tile<T, I, MODE_FUSED, A>(a, s);
 }
