@@ -16,19 +16,26 @@
 // the few centroids that can still win (recheck kernel), so labels never
 // drift from the plain form.
 //
-// Error bound (unscaled units, u = 2^-11 for fp16, 2^-8 for bf16, operands
-// scaled by a global power of two sigma, eta = 2^-25 the fp16 subnormal
-// half-spacing, d features):
-//   E_i = ||x_i||_2 * Cmax * kappa + (eta/sigma)(1+u)(||x_i||_1 + C1max)
-//         + d (eta/sigma)^2 + Hmax (u^3 + 2^-16) + 2^-13 / sigma^2
-//   kappa = 2u + u^2 + 2^-16 + (d + 4) 2^-23
-// with Cmax = max_j ||c_j||_2, C1max = max_j ||c_j||_1, Hmax = max_j |hn_j|.
-// It covers operand rounding (2u + u^2 per product), the three-part split of
-// the half norms (u^3, plus subnormal parts), tensor-core fp32 accumulation
+// Error bound (unscaled units; operands scaled by a global power of two
+// sigma and rounded to 16 bits: sigma x + dX_i and sigma c_j + dC_j, where the
+// rounding errors dX_i, dC_j are exact in fp32 and measured, subnormals
+// included; u = 2^-11 for fp16, 2^-8 for bf16; d features):
+//   E_i = ||x_i|| alpha + ||dX_i|| / sigma beta1 + beta0
+//   alpha = dCmax + 2^-16 (Cmax + dCmax) + (d + 4) 2^-23 Cmax
+//   beta1 = (Cmax + dCmax)(1 + 2^-16)
+//   beta0 = Hmax (u^3 + 2^-16 + 2^-23) + hfloor
+// with Cmax = max_j ||c_j||, dCmax = max_j ||dC_j|| / sigma, Hmax = max_j
+// |hn_j|.  By Cauchy-Schwarz |(sigma x + dX).(sigma c + dC) - sigma^2 x.c| <=
+// ||dX|| (||sigma c|| + ||dC||) + ||sigma x|| ||dC||: the measured rounding
+// errors (about 0.4 u ||.|| for random data) replace the worst case u ||.||
+// of each operand.  The bound also covers the three-part split of the half
+// norms (u^3, plus subnormal parts hfloor), tensor-core fp32 accumulation
 // (<= 2^-17 relative to the sum of magnitudes, allowing truncation), and the
-// reference's sequential fp32 dot (d 2^-24) and final subtraction.  All norms
-// are rounded up.  sigma keeps |x sigma| <= 2^14 and sigma^2 * hn <= 2^25 so
-// every 16-bit part is finite.
+// reference's sequential fp32 dot (d 2^-24) and final subtraction; for bf16,
+// whose subnormal inputs the tensor cores may flush, 2^-126 sqrt(d) (1 + u)
+// is added to alpha and that times Cmax to beta0.  All norms are rounded up.
+// sigma keeps |x sigma| <= 2^14 and sigma^2 * hn <= 2^25 so every 16-bit part
+// is finite.
 //
 // Runner-up without sorting: per sample, P1[s] = max over 32-column
 // sub-chunk s and P2[t] = max over columns j = t (mod 32).  Two distinct
@@ -75,7 +82,7 @@ constexpr size_t kSmemLimit = 232448;
 
 struct MixedConsts {
     float s2;       // sigma^2 (scores in TMEM are sigma^2 (x.c - hn))
-    float alpha;    // E_i = nx_i * alpha + n1_i * beta1 + beta0
+    float alpha;    // E_i = nx_i * alpha + ndx_i * beta1 + beta0
     float beta1;
     float beta0;
     float sigma;
@@ -88,7 +95,7 @@ struct MixedArgs {
     const uint8_t *ximg;
     const uint8_t *cimg;
     const float *nx;
-    const float *n1;
+    const float *ndx;   // ||operand rounding error of x_i|| / sigma, rounded up
     const MixedConsts *consts;
     const float *X;
     const float *w;
@@ -386,26 +393,26 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
         uint32_t cnt = 0;
         int tl = 0;
         // per-sample norms of the next tile are loaded one tile ahead
-        float nx_next = 0.f, n1_next = 0.f;
+        float nx_next = 0.f, dx_next = 0.f;
         {
             const int64_t i0 = (int64_t)blockIdx.x * kTileM + row;
             if (i0 < n) {
                 nx_next = a.nx[i0];
-                n1_next = a.n1[i0];
+                dx_next = a.ndx[i0];
             }
         }
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tl) {
             const int64_t i = tile * kTileM + row;
             float E2 = 0.f;
             if (i < n) {
-                const float e = fmaf(nx_next, cst.alpha, fmaf(n1_next, cst.beta1, cst.beta0));
+                const float e = fmaf(nx_next, cst.alpha, fmaf(dx_next, cst.beta1, cst.beta0));
                 E2 = 2.f * e * 1.000001f;
             }
             {
                 const int64_t inext = (tile + gridDim.x) * kTileM + row;
                 if (inext < n) {
                     nx_next = a.nx[inext];
-                    n1_next = a.n1[inext];
+                    dx_next = a.ndx[inext];
                 }
             }
             float P2[32], P1[kP1s ? 1 : kSub];
@@ -650,20 +657,27 @@ __global__ void sigma_kernel(MixedConsts *c, int bf16, int64_t d) {
     c->overflow = 0;
 }
 
+// Round to the 16-bit operand type and back (exact in fp32).
+template <int BF16>
+__device__ __forceinline__ float round16(float v) {
+    if (BF16) return __bfloat162float(__float2bfloat16_rn(v));
+    return __half2float(__float2half_rn(v));
+}
+
 // One thread per sample row (including the zero rows that pad the last
 // tile): the 128-byte-swizzled K-major image of (x * sigma), the row-major
-// fp32 copy of x (features d..d4-1 zero), and the norms ||x||_2, ||x||_1
-// rounded up.
+// fp32 copy of x (features d..d4-1 zero), ||x|| and the norm of the image's
+// rounding error ||round16(x sigma) - x sigma|| / sigma, both rounded up.
 template <int BF16>
 __global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int64_t d4, int nkb,
                                int64_t rows, const MixedConsts *c, uint8_t *img, float *xrow,
-                               float *nx, float *n1) {
+                               float *nx, float *ndx) {
     const float sigma = c->sigma;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t tile = i / kTileM;
         const uint32_t r = (uint32_t)(i % kTileM);
-        float s2 = 0.f, s1 = 0.f;  // float32 sums, bounded from above below
+        float s2 = 0.f, sd = 0.f;  // float32 sums, bounded from above below
         for (int kb = 0; kb < nkb; ++kb) {
             uint8_t *base = img + ((size_t)tile * nkb + kb) * kTileBytes;
             for (int ch = 0; ch < 8; ++ch) {
@@ -673,8 +687,9 @@ __global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int64_t d4,
                     const int64_t f = (int64_t)kb * 64 + ch * 8 + e;
                     const float x = (i < n && f < d) ? X[f * n + i] : 0.f;
                     s2 = __fmaf_rn(x, x, s2);
-                    s1 = __fadd_rn(s1, fabsf(x));
                     v[e] = x * sigma;
+                    const float dv = round16<BF16>(v[e]) - v[e];  // exact
+                    sd = __fmaf_rn(dv, dv, sd);
                     xr[e] = x;
                 }
                 if (i < n) {
@@ -695,19 +710,13 @@ __global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int64_t d4,
             // A float32 sum of m non-negative terms (each rounded once) is at
             // least (1 - 2^-24)^m times the exact sum; m <= 128 here, so the
             // factor 1 + (m + 2) 2^-23 applied with upward rounding (and an
-            // upward square root) gives upper bounds of ||x||_2 and ||x||_1.
+            // upward square root) gives upper bounds of both norms (1 / sigma
+            // is a power of two).
             const float grow = 1.f + (float)(nkb * 64 + 2) * 0x1p-23f;
             nx[i] = __fsqrt_ru(__fmul_ru(s2, grow));
-            n1[i] = __fmul_ru(s1, grow);
+            ndx[i] = __fmul_ru(__fsqrt_ru(__fmul_ru(sd, grow)), 1.f / sigma);
         }
     }
-}
-
-// Round to the 16-bit operand type and back (exact in fp32).
-template <int BF16>
-__device__ __forceinline__ float round16(float v) {
-    if (BF16) return __bfloat162float(__float2bfloat16_rn(v));
-    return __half2float(__float2half_rn(v));
 }
 
 // Largest finite operand value: fp16 65504, bf16 (1 - 2^-8) 2^128.
@@ -717,7 +726,8 @@ __device__ __forceinline__ float max16() {
 }
 
 // Centroid image (rows j < k_pad, zero padding), the half-norm block and the
-// per-centroid norms.  Row j of the half-norm block holds (h0, h1, h2) with
+// per-centroid norms ||c_j|| and ||round16(c_j sigma) - c_j sigma|| / sigma
+// (both rounded up).  Row j of the half-norm block holds (h0, h1, h2) with
 //   c0 h0 + c1 h1 + c2 h2 = -sigma^2 hn_j   (c = norm_coef)
 // up to sigma^2 |hn_j| u^3 (u = 2^-11 fp16, 2^-8 bf16; plus 2^-35 for fp16
 // subnormal parts): h0 is the rounded leading part and each following part
@@ -727,7 +737,7 @@ __device__ __forceinline__ float max16() {
 template <int BF16>
 __global__ void c_image_kernel(const float *C, const float *hn, int64_t d, int64_t k,
                                int64_t k_pad, int nkb, MixedConsts *c, uint8_t *img, float *cn2,
-                               float *cn1, float *ct, int64_t d4, const LoopState *guard) {
+                               float *dcn, float *ct, int64_t d4, const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
     const float sigma = c->sigma;
     const double s2 = (double)sigma * (double)sigma;
@@ -735,7 +745,7 @@ __global__ void c_image_kernel(const float *C, const float *hn, int64_t d, int64
     bool ovf = false;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < k_pad;
          j += (int64_t)gridDim.x * blockDim.x) {
-        double q2 = 0.0, q1 = 0.0;
+        double q2 = 0.0, qd = 0.0;
         for (int kb = 0; kb < nkb; ++kb) {
             uint8_t *base = img + (size_t)kb * k_pad * 128;
             for (int ch = 0; ch < 8; ++ch) {
@@ -745,12 +755,13 @@ __global__ void c_image_kernel(const float *C, const float *hn, int64_t d, int64
                     const int64_t f = (int64_t)kb * 64 + ch * 8 + e;
                     const float x = (j < k && f < d) ? C[f * k + j] : 0.f;
                     q2 += (double)x * (double)x;
-                    q1 += fabs((double)x);
                     float sv = x * sigma;
                     if (!(fabsf(sv) <= lim)) {
                         ovf = true;
                         sv = (sv > 0.f) ? lim : ((sv < 0.f) ? -lim : 0.f);
                     }
+                    const double dv = (double)round16<BF16>(sv) - (double)sv;
+                    qd += dv * dv;
                     v[e] = sv;
                     if (f < d4) ct[j * d4 + f] = x;
                 }
@@ -782,7 +793,7 @@ __global__ void c_image_kernel(const float *C, const float *hn, int64_t d, int64
                 h2 = 0.f;
             }
             cn2[j] = __double2float_ru(sqrt(q2) * (1.0 + 1e-12));
-            cn1[j] = __double2float_ru(q1 * (1.0 + 1e-12));
+            dcn[j] = __double2float_ru(sqrt(qd) / (double)sigma * (1.0 + 1e-12));
         }
         uint8_t *nb = img + (size_t)nkb * k_pad * 128;
         uint4 p0 = make_uint4(pack2<BF16>(h0, h1), pack2<BF16>(h2, 0.f), 0u, 0u);
@@ -794,14 +805,14 @@ __global__ void c_image_kernel(const float *C, const float *hn, int64_t d, int64
 
 // Per-iteration bound constants (one block), in the scaled units of the
 // scores (sigma^2).  Resets the overflow flag raised by c_image_kernel.
-__global__ void bound_kernel(const float *cn2, const float *cn1, const float *hn, int64_t d,
+__global__ void bound_kernel(const float *cn2, const float *dcn, const float *hn, int64_t d,
                              int64_t k, int bf16, MixedConsts *c, const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
     __shared__ float sh[3][32];
     float m2 = 0.f, m1 = 0.f, mh = 0.f;
     for (int64_t j = threadIdx.x; j < k; j += blockDim.x) {
         m2 = fmaxf(m2, cn2[j]);
-        m1 = fmaxf(m1, cn1[j]);
+        m1 = fmaxf(m1, dcn[j]);
         mh = fmaxf(mh, fabsf(hn[j]));
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -824,15 +835,16 @@ __global__ void bound_kernel(const float *cn2, const float *cn1, const float *hn
         }
         const double sigma = (double)c->sigma, s2 = sigma * sigma;
         const double u = bf16 ? 0x1p-8 : 0x1p-11;
-        // half-spacing of the operand type's subnormals (bf16: its smallest
-        // normal, in case the tensor cores flush bf16 subnormals)
-        const double eta = (bf16 ? 0x1p-126 : 0x1p-25) / sigma;
-        const double kappa = 2 * u + u * u + 0x1p-16 + (double)(d + 4) * 0x1p-23;
-        const double alpha = (double)m2 * kappa;
-        const double beta1 = eta * (1 + u);
+        const double cmax = (double)m2, dcmax = (double)m1;
+        // bf16 subnormal inputs may be flushed by the tensor cores (fp16
+        // subnormals are part of the measured rounding errors)
+        const double flush = bf16 ? 0x1p-126 * sqrt((double)d) * (1 + u) : 0.0;
+        const double alpha =
+            dcmax + 0x1p-16 * (cmax + dcmax) + (double)(d + 4) * 0x1p-23 * cmax + flush;
+        const double beta1 = (cmax + dcmax) * (1 + 0x1p-16);
         const double hfloor = (bf16 ? 0x1p-126 : 0x1p-34) / s2;
-        const double beta0 = beta1 * (double)m1 + (double)d * eta * eta +
-                             (double)mh * (u * u * u + 0x1p-16 + 0x1p-23) + hfloor;
+        const double beta0 =
+            (double)mh * (u * u * u + 0x1p-16 + 0x1p-23) + hfloor + flush * cmax;
         c->alpha = __double2float_ru(alpha * s2 * (1 + 1e-6));
         c->beta1 = __double2float_ru(beta1 * s2 * (1 + 1e-6));
         c->beta0 = c->overflow ? pos_inf<float>()
@@ -1013,11 +1025,11 @@ struct MixedFit : PlainFit<float, I> {
     int64_t k_pad = 0, d4 = 0, ntiles = 0;
     Scratch mws;
     uint8_t *ximg = nullptr, *cimg = nullptr;
-    float *nx = nullptr, *n1 = nullptr, *ct = nullptr, *xrow = nullptr;
+    float *nx = nullptr, *ndx = nullptr, *ct = nullptr, *xrow = nullptr;
     float *sums32 = nullptr;
     double *acc64 = nullptr;
     int n_copies = 1;  // private copies of the cluster sums (one per CTA)
-    float *cn2 = nullptr, *cn1 = nullptr;
+    float *cn2 = nullptr, *dcn = nullptr;
     MixedConsts *consts = nullptr;
     uint4 *cand = nullptr;
     int *flagged = nullptr, *n_flagged = nullptr, *err_dev = nullptr;
@@ -1064,7 +1076,7 @@ struct MixedFit : PlainFit<float, I> {
         const size_t o_c = take(cimg_bytes(nkb, k_pad));
         const size_t o_ct = take(sizeof(float) * k_pad * d4);
         const size_t o_nx = take(sizeof(float) * p.n);
-        const size_t o_n1 = take(sizeof(float) * p.n);
+        const size_t o_ndx = take(sizeof(float) * p.n);
         // Small sums get one private copy per CTA of the assignment: their
         // few addresses would otherwise serialise the reductions of all SMs.
         // Large ones (c3-sized, 266 KB) stay single: per-CTA copies would
@@ -1077,7 +1089,7 @@ struct MixedFit : PlainFit<float, I> {
         const size_t o_a64 = take(acc_f64 ? sizeof(double) * csz : 16);
         const size_t o_xf = take(sizeof(float) * std::max<int64_t>(p.n, 1) * d4);
         const size_t o_cn2 = take(sizeof(float) * p.k);
-        const size_t o_cn1 = take(sizeof(float) * p.k);
+        const size_t o_dcn = take(sizeof(float) * p.k);
         const size_t o_cst = take(sizeof(MixedConsts));
         const size_t o_cand = take(sizeof(uint4) * p.n);
         const size_t o_flg = take(sizeof(int) * p.n);
@@ -1089,12 +1101,12 @@ struct MixedFit : PlainFit<float, I> {
         cimg = reinterpret_cast<uint8_t *>(b + o_c);
         ct = reinterpret_cast<float *>(b + o_ct);
         nx = reinterpret_cast<float *>(b + o_nx);
-        n1 = reinterpret_cast<float *>(b + o_n1);
+        ndx = reinterpret_cast<float *>(b + o_ndx);
         sums32 = reinterpret_cast<float *>(b + o_s32);
         acc64 = reinterpret_cast<double *>(b + o_a64);
         xrow = reinterpret_cast<float *>(b + o_xf);
         cn2 = reinterpret_cast<float *>(b + o_cn2);
-        cn1 = reinterpret_cast<float *>(b + o_cn1);
+        dcn = reinterpret_cast<float *>(b + o_dcn);
         consts = reinterpret_cast<MixedConsts *>(b + o_cst);
         cand = reinterpret_cast<uint4 *>(b + o_cand);
         flagged = reinterpret_cast<int *>(b + o_flg);
@@ -1113,10 +1125,10 @@ struct MixedFit : PlainFit<float, I> {
         const int64_t rows = ntiles * kTileM;
         if (bf16)
             x_image_kernel<1><<<grid1d(rows, 256, 1 << 20), 256, 0, s>>>(
-                p.X, p.n, p.d, d4, nkb, rows, consts, ximg, xrow, nx, n1);
+                p.X, p.n, p.d, d4, nkb, rows, consts, ximg, xrow, nx, ndx);
         else
             x_image_kernel<0><<<grid1d(rows, 256, 1 << 20), 256, 0, s>>>(
-                p.X, p.n, p.d, d4, nkb, rows, consts, ximg, xrow, nx, n1);
+                p.X, p.n, p.d, d4, nkb, rows, consts, ximg, xrow, nx, ndx);
         KMC_TRY(check_launch("x_image"));
         this->launches += 3;
         return KMC_OK;
@@ -1127,12 +1139,12 @@ struct MixedFit : PlainFit<float, I> {
         cudaStream_t s = p.stream;
         if (bf16)
             c_image_kernel<1><<<grid1d(k_pad, 128, 4096), 128, 0, s>>>(
-                cur, this->hn, p.d, p.k, k_pad, nkb, consts, cimg, cn2, cn1, ct, d4, guard);
+                cur, this->hn, p.d, p.k, k_pad, nkb, consts, cimg, cn2, dcn, ct, d4, guard);
         else
             c_image_kernel<0><<<grid1d(k_pad, 128, 4096), 128, 0, s>>>(
-                cur, this->hn, p.d, p.k, k_pad, nkb, consts, cimg, cn2, cn1, ct, d4, guard);
+                cur, this->hn, p.d, p.k, k_pad, nkb, consts, cimg, cn2, dcn, ct, d4, guard);
         KMC_TRY(check_launch("c_image"));
-        bound_kernel<<<1, 1024, 0, s>>>(cn2, cn1, this->hn, p.d, p.k, bf16, consts, guard);
+        bound_kernel<<<1, 1024, 0, s>>>(cn2, dcn, this->hn, p.d, p.k, bf16, consts, guard);
         return check_launch("bound");
     }
 
@@ -1148,7 +1160,7 @@ struct MixedFit : PlainFit<float, I> {
         a.ximg = ximg;
         a.cimg = cimg;
         a.nx = nx;
-        a.n1 = n1;
+        a.ndx = ndx;
         a.consts = consts;
         a.X = p.X;
         a.w = p.w;
