@@ -856,88 +856,146 @@ __global__ void bound_kernel(const float *cn2, const float *dcn, const float *hn
 // Exact fp32 re-evaluation of samples whose margin did not certify them: the
 // reference's arithmetic (sequential fma dot over f = 0..d-1, hn - dot,
 // strict < with the lowest index on ties) over the candidate set (hot
-// sub-chunks x hot classes of each column half), one thread per sample so
-// that thousands of samples are in flight.  The sample's features come from
-// the row-major fp32 copy of X (cached in L1 across its candidates) and the
+// sub-chunks x hot classes of each column half).  A warp takes 32 flagged
+// samples and spreads their (sample, candidate) pairs evenly over its lanes,
+// so one sample with many candidates does not hold its warp back; each pair's
+// result goes into the sample's 64-bit (distance, index) key with a
+// shared-memory atomic minimum, which is exactly the lexicographic minimum a
+// strict-< scan in ascending index finds.  The sample's features come from the
+// row-major fp32 copy of X (cached in L1 across its candidates) and the
 // centroids from their transposed fp32 copy (one contiguous row each).
-__global__ void __launch_bounds__(256) recheck_kernel(
+constexpr int kRecheckThreads = 256;
+
+// Order-preserving map of a float to an unsigned key (NaN never compared).
+__device__ __forceinline__ uint32_t order_key(float v) {
+    const uint32_t u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void __launch_bounds__(kRecheckThreads) recheck_kernel(
     const float *xrow, const float *ct, const float *hn, const float *w, const uint4 *cand,
     const int *flagged, const int *n_flagged, int64_t n, int64_t d, int64_t k, int64_t d4,
     void *labels, int label64, int update, int acc_f64, float *sums32, double *acc64,
     int64_t k_pad, int n_copies, const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
+    constexpr int kWarps = kRecheckThreads / 32;
+    __shared__ unsigned long long key_s[kWarps][32];
+    __shared__ int incl_s[kWarps][32];
+    __shared__ int row_s[kWarps][32];
+    __shared__ uint4 cm_s[kWarps][32];
     {
         // this block's share of the per-CTA copies of the cluster sums
         const int64_t copy = (int64_t)(blockIdx.x % (unsigned)n_copies) * (k_pad * d4 + k_pad);
         sums32 += copy;
         acc64 += copy;
     }
+    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
     const int64_t nf = (int64_t)*n_flagged;
     const int64_t total = nf < n ? nf : n;
     const int64_t g4 = d4 / 4;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = flagged[e];
-        if (i < 0 || i >= n) continue;
-        const float4 *xr = reinterpret_cast<const float4 *>(xrow + i * d4);
-        const uint4 cm = cand[i];
-        float best = pos_inf<float>();
-        int bj = 0;
+    const unsigned long long kNone = ((unsigned long long)order_key(pos_inf<float>()) << 32);
+    const int64_t wstride = (int64_t)gridDim.x * kWarps * 32;
+    for (int64_t base = ((int64_t)blockIdx.x * kWarps + wq) * 32; base < total; base += wstride) {
+        const int64_t e = base + lane;
+        int64_t i = -1;
+        uint4 cm = make_uint4(0u, 0u, 0u, 0u);
+        if (e < total) {
+            i = flagged[e];
+            if (i >= 0 && i < n) cm = cand[i];
+            else i = -1;
+        }
+        // candidates of this lane's sample: per column half, hot sub-chunks x hot classes
+        const int c0 = __popc(cm.x) * __popc(cm.z);
+        const int cnt = c0 + __popc(cm.y) * __popc(cm.w);
+        int incl = cnt;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const uint32_t m1 = h ? cm.y : cm.x, m2 = h ? cm.w : cm.z;
-            for (uint32_t a1 = m1; a1 != 0u; a1 &= a1 - 1u) {
-                const int sc = __ffs(a1) - 1;
-                for (uint32_t a2 = m2; a2 != 0u; a2 &= a2 - 1u) {
-                    const int t = __ffs(a2) - 1;
-                    const int64_t j = (int64_t)(sc >> 2) * kChunkN + h * 128 + (sc & 3) * 32 + t;
-                    if (j >= k) continue;
-                    const float4 *cr = reinterpret_cast<const float4 *>(ct + j * d4);
-                    float dot = 0.f;
-                    // unrolled so that a candidate's row loads are in flight
-                    // before its fma chain needs them
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int tot = __shfl_sync(0xffffffffu, incl, 31);
+        key_s[wq][lane] = kNone;
+        incl_s[wq][lane] = incl;
+        row_s[wq][lane] = (int)i;
+        cm_s[wq][lane] = cm;
+        __syncwarp();
+        for (int pr = lane; pr < tot; pr += 32) {
+            // owner: the first lane whose inclusive count exceeds pr
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (incl_s[wq][mid] > pr) hi = mid; else lo = mid + 1;
+            }
+            const int owner = lo;
+            int r = pr - (owner ? incl_s[wq][owner - 1] : 0);
+            const uint4 om = cm_s[wq][owner];
+            const int oc0 = __popc(om.x) * __popc(om.z);
+            int h = 0;
+            uint32_t m1 = om.x, m2 = om.z;
+            if (r >= oc0) {
+                h = 1;
+                r -= oc0;
+                m1 = om.y;
+                m2 = om.w;
+            }
+            // the (r / n2)-th hot sub-chunk and the (r % n2)-th hot class
+            const int n2 = __popc(m2);
+            for (int q = r / n2; q > 0; --q) m1 &= m1 - 1u;
+            for (int q = r % n2; q > 0; --q) m2 &= m2 - 1u;
+            const int sc = __ffs(m1) - 1, t = __ffs(m2) - 1;
+            const int64_t j = (int64_t)(sc >> 2) * kChunkN + h * 128 + (sc & 3) * 32 + t;
+            if (j >= k) continue;
+            const int64_t oi = row_s[wq][owner];
+            const float4 *xr = reinterpret_cast<const float4 *>(xrow + oi * d4);
+            const float4 *cr = reinterpret_cast<const float4 *>(ct + j * d4);
+            float dot = 0.f;
+            // unrolled so that a candidate's row loads are in flight
+            // before its fma chain needs them
 #pragma unroll 8
+            for (int64_t g = 0; g < g4; ++g) {
+                const float4 xv = __ldg(xr + g), cv = __ldg(cr + g);
+                dot = __fmaf_rn(xv.x, cv.x, dot);
+                if (4 * g + 1 < d) dot = __fmaf_rn(xv.y, cv.y, dot);
+                if (4 * g + 2 < d) dot = __fmaf_rn(xv.z, cv.z, dot);
+                if (4 * g + 3 < d) dot = __fmaf_rn(xv.w, cv.w, dot);
+            }
+            const float D = hn[j] - dot;
+            if (D == D)
+                atomicMin(&key_s[wq][owner],
+                          ((unsigned long long)order_key(D) << 32) | (unsigned long long)j);
+        }
+        __syncwarp();
+        if (i >= 0) {
+            const int bj = (int)(key_s[wq][lane] & 0xffffffffull);
+            if (label64)
+                reinterpret_cast<int64_t *>(labels)[i] = bj;
+            else
+                reinterpret_cast<int32_t *>(labels)[i] = bj;
+            if (update) {
+                const float4 *xr = reinterpret_cast<const float4 *>(xrow + i * d4);
+                const float wv = w[i];
+                if (acc_f64) {
+                    double *dst = acc64 + (int64_t)bj * d4;
                     for (int64_t g = 0; g < g4; ++g) {
-                        const float4 xv = __ldg(xr + g), cv = __ldg(cr + g);
-                        dot = __fmaf_rn(xv.x, cv.x, dot);
-                        if (4 * g + 1 < d) dot = __fmaf_rn(xv.y, cv.y, dot);
-                        if (4 * g + 2 < d) dot = __fmaf_rn(xv.z, cv.z, dot);
-                        if (4 * g + 3 < d) dot = __fmaf_rn(xv.w, cv.w, dot);
+                        const float4 xv = __ldg(xr + g);
+                        atomicAdd(dst + 4 * g + 0, (double)__fmul_rn(xv.x, wv));
+                        atomicAdd(dst + 4 * g + 1, (double)__fmul_rn(xv.y, wv));
+                        atomicAdd(dst + 4 * g + 2, (double)__fmul_rn(xv.z, wv));
+                        atomicAdd(dst + 4 * g + 3, (double)__fmul_rn(xv.w, wv));
                     }
-                    const float D = hn[j] - dot;
-                    if (D < best || (D == best && j < bj)) {
-                        best = D;
-                        bj = (int)j;
+                    atomicAdd(acc64 + k_pad * d4 + bj, (double)wv);
+                } else {
+                    float4 *dst = reinterpret_cast<float4 *>(sums32 + (int64_t)bj * d4);
+                    for (int64_t g = 0; g < g4; ++g) {
+                        const float4 xv = __ldg(xr + g);
+                        atomicAdd(dst + g, make_float4(__fmul_rn(xv.x, wv), __fmul_rn(xv.y, wv),
+                                                       __fmul_rn(xv.z, wv), __fmul_rn(xv.w, wv)));
                     }
+                    atomicAdd(sums32 + k_pad * d4 + bj, wv);
                 }
             }
         }
-        if (label64)
-            reinterpret_cast<int64_t *>(labels)[i] = bj;
-        else
-            reinterpret_cast<int32_t *>(labels)[i] = bj;
-        if (update) {
-            const float wv = w[i];
-            if (acc_f64) {
-                double *dst = acc64 + (int64_t)bj * d4;
-                for (int64_t g = 0; g < g4; ++g) {
-                    const float4 xv = __ldg(xr + g);
-                    atomicAdd(dst + 4 * g + 0, (double)__fmul_rn(xv.x, wv));
-                    atomicAdd(dst + 4 * g + 1, (double)__fmul_rn(xv.y, wv));
-                    atomicAdd(dst + 4 * g + 2, (double)__fmul_rn(xv.z, wv));
-                    atomicAdd(dst + 4 * g + 3, (double)__fmul_rn(xv.w, wv));
-                }
-                atomicAdd(acc64 + k_pad * d4 + bj, (double)wv);
-            } else {
-                float4 *dst = reinterpret_cast<float4 *>(sums32 + (int64_t)bj * d4);
-                for (int64_t g = 0; g < g4; ++g) {
-                    const float4 xv = __ldg(xr + g);
-                    atomicAdd(dst + g, make_float4(__fmul_rn(xv.x, wv), __fmul_rn(xv.y, wv),
-                                                   __fmul_rn(xv.z, wv), __fmul_rn(xv.w, wv)));
-                }
-                atomicAdd(sums32 + k_pad * d4 + bj, wv);
-            }
-        }
+        __syncwarp();  // the keys and masks of this round are read before the next one
     }
 }
 
@@ -1197,7 +1255,7 @@ struct MixedFit : PlainFit<float, I> {
             kern<<<(unsigned)grid, kThreadsMixed, L.total, s>>>(a);
             KMC_TRY(check_launch("mixed_assign"));
         }
-        recheck_kernel<<<(unsigned)(num_sms() * 8), 256, 0, s>>>(
+        recheck_kernel<<<(unsigned)(num_sms() * 8), kRecheckThreads, 0, s>>>(
             xrow, ct, this->hn, p.w, cand, flagged, n_flagged, p.n, p.d, p.k, d4, p.labels,
             a.label64, update, acc_f64, sums32, acc64, k_pad, n_copies, guard);
         KMC_TRY(check_launch("mixed_recheck"));
