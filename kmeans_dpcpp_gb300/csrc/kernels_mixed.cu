@@ -743,36 +743,50 @@ __global__ void c_image_kernel(const float *C, const float *hn, int64_t d, int64
     const double s2 = (double)sigma * (double)sigma;
     const float lim = max16<BF16>();
     bool ovf = false;
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < k_pad;
-         j += (int64_t)gridDim.x * blockDim.x) {
+    // One thread per (centroid row j, 8-feature chunk): G = 8 nkb consecutive
+    // lanes hold one row (k_pad G is a multiple of 32, so every warp is either
+    // entirely inside the range or entirely past it).
+    const int G = 8 * nkb;
+    const int64_t total = k_pad * G;
+    for (int64_t tt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; tt < total;
+         tt += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = tt / G;
+        const int qc = (int)(tt % G), kb = qc >> 3, ch = qc & 7;
+        const int64_t f0 = (int64_t)kb * 64 + ch * 8;
         double q2 = 0.0, qd = 0.0;
-        for (int kb = 0; kb < nkb; ++kb) {
-            uint8_t *base = img + (size_t)kb * k_pad * 128;
-            for (int ch = 0; ch < 8; ++ch) {
-                float v[8];
+        float v[8], xr[8];
 #pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    const int64_t f = (int64_t)kb * 64 + ch * 8 + e;
-                    const float x = (j < k && f < d) ? C[f * k + j] : 0.f;
-                    q2 += (double)x * (double)x;
-                    float sv = x * sigma;
-                    if (!(fabsf(sv) <= lim)) {
-                        ovf = true;
-                        sv = (sv > 0.f) ? lim : ((sv < 0.f) ? -lim : 0.f);
-                    }
-                    const double dv = (double)round16<BF16>(sv) - (double)sv;
-                    qd += dv * dv;
-                    v[e] = sv;
-                    if (f < d4) ct[j * d4 + f] = x;
-                }
-                uint4 pk;
-                pk.x = pack2<BF16>(v[0], v[1]);
-                pk.y = pack2<BF16>(v[2], v[3]);
-                pk.z = pack2<BF16>(v[4], v[5]);
-                pk.w = pack2<BF16>(v[6], v[7]);
-                *reinterpret_cast<uint4 *>(base + sw128_offset((uint32_t)j, (uint32_t)ch * 8)) = pk;
+        for (int e = 0; e < 8; ++e) {
+            const int64_t f = f0 + e;
+            const float x = (j < k && f < d) ? C[f * k + j] : 0.f;
+            q2 += (double)x * (double)x;
+            float sv = x * sigma;
+            if (!(fabsf(sv) <= lim)) {
+                ovf = true;
+                sv = (sv > 0.f) ? lim : ((sv < 0.f) ? -lim : 0.f);
             }
+            const double dv = (double)round16<BF16>(sv) - (double)sv;
+            qd += dv * dv;
+            v[e] = sv;
+            xr[e] = x;
         }
+        // d4 is a multiple of 4 and f0 of 8: whole float4 stores
+        float4 *cdst = reinterpret_cast<float4 *>(ct + j * d4 + f0);
+        if (f0 < d4) cdst[0] = make_float4(xr[0], xr[1], xr[2], xr[3]);
+        if (f0 + 4 < d4) cdst[1] = make_float4(xr[4], xr[5], xr[6], xr[7]);
+        uint4 pk;
+        pk.x = pack2<BF16>(v[0], v[1]);
+        pk.y = pack2<BF16>(v[2], v[3]);
+        pk.z = pack2<BF16>(v[4], v[5]);
+        pk.w = pack2<BF16>(v[6], v[7]);
+        *reinterpret_cast<uint4 *>(img + (size_t)kb * k_pad * 128 +
+                                   sw128_offset((uint32_t)j, (uint32_t)ch * 8)) = pk;
+        // the row's squared norms over its G chunk lanes
+        for (int o = G >> 1; o > 0; o >>= 1) {
+            q2 += __shfl_xor_sync(0xffffffffu, q2, o);
+            qd += __shfl_xor_sync(0xffffffffu, qd, o);
+        }
+        if (qc != 0) continue;
         float h0 = 0.f, h1 = 0.f, h2 = 0.f;
         if (j < k) {
             const double H = (double)hn[j] * s2;
@@ -1196,10 +1210,10 @@ struct MixedFit : PlainFit<float, I> {
         const FitParams<float, I> &p = this->prm;
         cudaStream_t s = p.stream;
         if (bf16)
-            c_image_kernel<1><<<grid1d(k_pad, 128, 4096), 128, 0, s>>>(
+            c_image_kernel<1><<<grid1d(k_pad * 8 * nkb, 128, 4096), 128, 0, s>>>(
                 cur, this->hn, p.d, p.k, k_pad, nkb, consts, cimg, cn2, dcn, ct, d4, guard);
         else
-            c_image_kernel<0><<<grid1d(k_pad, 128, 4096), 128, 0, s>>>(
+            c_image_kernel<0><<<grid1d(k_pad * 8 * nkb, 128, 4096), 128, 0, s>>>(
                 cur, this->hn, p.d, p.k, k_pad, nkb, consts, cimg, cn2, dcn, ct, d4, guard);
         KMC_TRY(check_launch("c_image"));
         bound_kernel<<<1, 1024, 0, s>>>(cn2, dcn, this->hn, p.d, p.k, bf16, consts, guard);

@@ -123,18 +123,35 @@ __global__ void shifts_kernel(const T *old_c, const T *new_c, T *out, int64_t d,
 // Driver fusion of broadcast_division_kernel (util_kernels.hpp:9-41) and the
 // shift kernel above: same per-element operations, one pass over (d, k).
 template <typename T>
-__global__ void divide_and_shift_kernel(const T *old_c, T *new_c, const T *sizes, T *shifts,
+__global__ void divide_and_shift_kernel(const T *__restrict__ old_c, T *__restrict__ new_c,
+                                        const T *__restrict__ sizes, T *__restrict__ shifts,
                                         int64_t d, int64_t k, const LoopState *guard) {
     if (stopped(guard)) return;
     int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= k) return;
     T sz = sizes[j];
     T acc = T(0);
-    for (int64_t f = 0; f < d; ++f) {
-        T c = new_c[f * k + j] / sz;
-        new_c[f * k + j] = c;
-        T diff = old_c[f * k + j] - c;
-        acc = fma_t(diff, diff, acc);
+    // features in groups of 8: the group's loads are all in flight before
+    // its divisions and the (sequential, as the reference's) fma chain
+    constexpr int kG = 8;
+    for (int64_t f0 = 0; f0 < d; f0 += kG) {
+        T nv[kG], ov[kG];
+#pragma unroll
+        for (int e = 0; e < kG; ++e) {
+            const int64_t f = f0 + e;
+            nv[e] = (f < d) ? new_c[f * k + j] : T(0);
+            ov[e] = (f < d) ? old_c[f * k + j] : T(0);
+        }
+#pragma unroll
+        for (int e = 0; e < kG; ++e) {
+            const int64_t f = f0 + e;
+            if (f < d) {
+                T c = nv[e] / sz;
+                new_c[f * k + j] = c;
+                T diff = ov[e] - c;
+                acc = fma_t(diff, diff, acc);
+            }
+        }
     }
     shifts[j] = acc;
 }
