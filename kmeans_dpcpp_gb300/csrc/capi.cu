@@ -38,6 +38,40 @@ int num_sms() {
     return cache[dev];
 }
 
+namespace {
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[64] = {};
+}  // namespace
+
+cudaMemPool_t scratch_pool() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (g_pools[dev] == nullptr) {
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;  // callers fall back to the device's default pool
+        }
+        uint64_t keep = ~uint64_t(0);
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        g_pools[dev] = pool;
+    }
+    return g_pools[dev];
+}
+
+int trim_pools() {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (int d = 0; d < 64; ++d)
+        if (g_pools[d] != nullptr) KMC_CUDA_TRY(cudaMemPoolTrimTo(g_pools[d], 0));
+    return KMC_OK;
+}
+
 int64_t l2_bytes() {
     int dev = 0, v = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
@@ -268,6 +302,7 @@ extern "C" {
 
 const char *kmc_last_error(void) { return kmc::get_error(); }
 int kmc_abi_version(void) { return 1; }
+int kmc_trim_cached_memory(void) { return kmc::trim_pools(); }
 
 #define KMC_T_ENTRY(SUF, T)                                                                    \
     int kmc_broadcast_divide_##SUF(T *X, const T *y, int64_t r, int64_t c, int64_t,            \

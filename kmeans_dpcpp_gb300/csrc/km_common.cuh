@@ -68,8 +68,16 @@ __host__ __device__ inline T pos_inf() { return std::numeric_limits<T>::infinity
 int num_sms();
 // L2 size in bytes of the current device.
 int64_t l2_bytes();
+// Returns the unused memory of the library's pools to the system.
+int trim_pools();
 
-// Stream-ordered scratch allocation (cudaMallocAsync on the caller's stream).
+// The library's own stream-ordered memory pool on the current device.  It
+// keeps freed memory mapped (release threshold = unlimited), so a fit that
+// follows another reuses the pages instead of mapping gigabytes again;
+// kmc_trim_cached_memory() hands the unused part back.
+cudaMemPool_t scratch_pool();
+
+// Stream-ordered scratch allocation (the library's pool, on the caller's stream).
 struct Scratch {
     void *ptr = nullptr;
     cudaStream_t stream = nullptr;
@@ -81,10 +89,13 @@ struct Scratch {
         ptr = nullptr;
         stream = s;
         if (bytes == 0) bytes = 16;
-        cudaError_t e = cudaMallocAsync(&ptr, bytes, s);
+        cudaMemPool_t pool = scratch_pool();
+        cudaError_t e = pool != nullptr ? cudaMallocFromPoolAsync(&ptr, bytes, pool, s)
+                                        : cudaMallocAsync(&ptr, bytes, s);
         if (e != cudaSuccess) {
             ptr = nullptr;
-            set_error("cudaMallocAsync(%zu) failed: %s", bytes, cudaGetErrorString(e));
+            set_error("stream-ordered allocation of %zu bytes failed: %s", bytes,
+                      cudaGetErrorString(e));
             return KMC_ERR_OUT_OF_MEMORY;
         }
         return KMC_OK;
