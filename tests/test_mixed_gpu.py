@@ -161,3 +161,18 @@ def test_mixed_iterations_match_oracle_step_by_step(oracle, case, form):
     np.testing.assert_array_equal(lab_final, oracle.assignment(X, C_final))
     inr_o = float(np.sum(oracle.compute_inertia(X, w, C_final, lab_final).astype(np.float64)))
     assert inertia.value == pytest.approx(inr_o, rel=1e-6)
+
+
+def test_fit_after_trimming_the_memory_pool_gives_the_same_labels(oracle):
+    """Scratch comes from a pool that keeps freed memory mapped; trimming it
+    between fits hands the memory back and the next fit allocates afresh."""
+    from kmeans_dpcpp_gb300 import capi
+
+    L = capi.lib()
+    X, _, _ = bench.make_blobs(20000, 64, 300, (-5, 5), 1.0, seed=11)
+    C0 = bench.random_row_init(X, 300, seed=11)
+    first = _fit_labels(X, C0, FORMS["fp16"])[1]
+    assert L.kmc_trim_cached_memory() == 0
+    second = _fit_labels(X, C0, FORMS["fp16"])[1]
+    np.testing.assert_array_equal(first, second)
+    np.testing.assert_array_equal(first, oracle.assignment(X, C0))
