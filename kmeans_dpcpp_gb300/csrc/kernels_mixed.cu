@@ -664,58 +664,79 @@ __device__ __forceinline__ float round16(float v) {
     return __half2float(__float2half_rn(v));
 }
 
-// One thread per sample row (including the zero rows that pad the last
-// tile): the 128-byte-swizzled K-major image of (x * sigma), the row-major
-// fp32 copy of x (features d..d4-1 zero), ||x|| and the norm of the image's
-// rounding error ||round16(x sigma) - x sigma|| / sigma, both rounded up.
+// One CTA per 128-sample tile (including the zero rows that pad the last
+// tile): the tile's features are staged in shared memory (coalesced reads of
+// each feature's 128 samples), then written out as the 128-byte-swizzled
+// K-major image of (x * sigma) and the row-major fp32 copy of x (features
+// d..d4-1 zero), both as contiguous 16-byte chunks, and per sample ||x|| and
+// the norm of the image's rounding error ||round16(x sigma) - x sigma|| /
+// sigma, both rounded up.
+constexpr int kXImageThreads = 256;
+constexpr int kXsPitch = kTileM + 1;  // floats per staged feature (bank offset)
+
+__host__ __device__ inline size_t x_image_smem(int nkb) {
+    return sizeof(float) * (size_t)nkb * 64 * kXsPitch;
+}
+
 template <int BF16>
-__global__ void x_image_kernel(const float *X, int64_t n, int64_t d, int64_t d4, int nkb,
-                               int64_t rows, const MixedConsts *c, uint8_t *img, float *xrow,
-                               float *nx, float *ndx) {
+__global__ void __launch_bounds__(kXImageThreads) x_image_kernel(
+    const float *X, int64_t n, int64_t d, int64_t d4, int nkb, int64_t ntiles,
+    const MixedConsts *c, uint8_t *img, float *xrow, float *nx, float *ndx) {
+    extern __shared__ float xs[];  // [feature][kXsPitch]
     const float sigma = c->sigma;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t tile = i / kTileM;
-        const uint32_t r = (uint32_t)(i % kTileM);
-        float s2 = 0.f, sd = 0.f;  // float32 sums, bounded from above below
-        for (int kb = 0; kb < nkb; ++kb) {
-            uint8_t *base = img + ((size_t)tile * nkb + kb) * kTileBytes;
-            for (int ch = 0; ch < 8; ++ch) {
-                float v[8], xr[8];
-#pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    const int64_t f = (int64_t)kb * 64 + ch * 8 + e;
-                    const float x = (i < n && f < d) ? X[f * n + i] : 0.f;
-                    s2 = __fmaf_rn(x, x, s2);
-                    v[e] = x * sigma;
-                    const float dv = round16<BF16>(v[e]) - v[e];  // exact
-                    sd = __fmaf_rn(dv, dv, sd);
-                    xr[e] = x;
-                }
-                if (i < n) {
-                    const int64_t f0 = (int64_t)kb * 64 + ch * 8;
-                    float4 *dst = reinterpret_cast<float4 *>(xrow + i * d4 + f0);
-                    if (f0 < d4) dst[0] = make_float4(xr[0], xr[1], xr[2], xr[3]);
-                    if (f0 + 4 < d4) dst[1] = make_float4(xr[4], xr[5], xr[6], xr[7]);
-                }
-                uint4 pk;
-                pk.x = pack2<BF16>(v[0], v[1]);
-                pk.y = pack2<BF16>(v[2], v[3]);
-                pk.z = pack2<BF16>(v[4], v[5]);
-                pk.w = pack2<BF16>(v[6], v[7]);
-                *reinterpret_cast<uint4 *>(base + sw128_offset(r, (uint32_t)ch * 8)) = pk;
-            }
+    const int F = nkb * 64;
+    const int g4 = (int)(d4 / 4);
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t i0 = tile * kTileM;
+        for (int e = threadIdx.x; e < F * kTileM; e += kXImageThreads) {
+            const int f = e >> 7, r = e & (kTileM - 1);
+            const int64_t i = i0 + r;
+            xs[f * kXsPitch + r] = (f < d && i < n) ? X[(int64_t)f * n + i] : 0.f;
         }
-        if (i < n) {
+        __syncthreads();
+        // image: 16-byte chunk q of feature block kb holds row r, features
+        // 8 ch .. 8 ch + 7 with ch = (q mod 8) xor (r mod 8) (128-byte swizzle)
+        for (int q = threadIdx.x; q < nkb * 1024; q += kXImageThreads) {
+            const int kb = q >> 10, qq = q & 1023;
+            const int r = (qq >> 6) * 8 + ((qq >> 3) & 7);
+            const int ch = (qq & 7) ^ (r & 7);
+            const float *src = xs + (kb * 64 + ch * 8) * kXsPitch + r;
+            uint4 pk;
+            pk.x = pack2<BF16>(src[0 * kXsPitch] * sigma, src[1 * kXsPitch] * sigma);
+            pk.y = pack2<BF16>(src[2 * kXsPitch] * sigma, src[3 * kXsPitch] * sigma);
+            pk.z = pack2<BF16>(src[4 * kXsPitch] * sigma, src[5 * kXsPitch] * sigma);
+            pk.w = pack2<BF16>(src[6 * kXsPitch] * sigma, src[7 * kXsPitch] * sigma);
+            *reinterpret_cast<uint4 *>(img + ((size_t)tile * nkb + kb) * kTileBytes +
+                                       (size_t)qq * 16) = pk;
+        }
+        // row-major fp32 rows: the tile's block of xrow is contiguous
+        const int rows_here = (n - i0 < (int64_t)kTileM) ? (int)(n - i0) : kTileM;
+        for (int e = threadIdx.x; e < rows_here * g4; e += kXImageThreads) {
+            const int r = e / g4, g = e - r * g4;
+            const float *src = xs + (4 * g) * kXsPitch + r;
+            reinterpret_cast<float4 *>(xrow + (i0 + r) * d4)[g] =
+                make_float4(src[0], src[kXsPitch], src[2 * kXsPitch], src[3 * kXsPitch]);
+        }
+        if (threadIdx.x < kTileM && threadIdx.x < rows_here) {
+            const int r = threadIdx.x;
+            float s2 = 0.f, sd = 0.f;  // float32 sums, bounded from above below
+            for (int f = 0; f < F; ++f) {
+                const float x = xs[f * kXsPitch + r];
+                s2 = __fmaf_rn(x, x, s2);
+                const float v = x * sigma;
+                const float dv = round16<BF16>(v) - v;  // exact
+                sd = __fmaf_rn(dv, dv, sd);
+            }
             // A float32 sum of m non-negative terms (each rounded once) is at
             // least (1 - 2^-24)^m times the exact sum; m <= 128 here, so the
             // factor 1 + (m + 2) 2^-23 applied with upward rounding (and an
             // upward square root) gives upper bounds of both norms (1 / sigma
             // is a power of two).
             const float grow = 1.f + (float)(nkb * 64 + 2) * 0x1p-23f;
-            nx[i] = __fsqrt_ru(__fmul_ru(s2, grow));
-            ndx[i] = __fmul_ru(__fsqrt_ru(__fmul_ru(sd, grow)), 1.f / sigma);
+            nx[i0 + r] = __fsqrt_ru(__fmul_ru(s2, grow));
+            ndx[i0 + r] = __fmul_ru(__fsqrt_ru(__fmul_ru(sd, grow)), 1.f / sigma);
         }
+        __syncthreads();
     }
 }
 
@@ -1194,13 +1215,16 @@ struct MixedFit : PlainFit<float, I> {
         KMC_TRY(check_launch("absmax"));
         sigma_kernel<<<1, 1, 0, s>>>(consts, bf16, p.d);
         KMC_TRY(check_launch("sigma"));
-        const int64_t rows = ntiles * kTileM;
-        if (bf16)
-            x_image_kernel<1><<<grid1d(rows, 256, 1 << 20), 256, 0, s>>>(
-                p.X, p.n, p.d, d4, nkb, rows, consts, ximg, xrow, nx, ndx);
-        else
-            x_image_kernel<0><<<grid1d(rows, 256, 1 << 20), 256, 0, s>>>(
-                p.X, p.n, p.d, d4, nkb, rows, consts, ximg, xrow, nx, ndx);
+        {
+            auto xk = bf16 ? x_image_kernel<1> : x_image_kernel<0>;
+            const size_t xsm = x_image_smem(nkb);
+            if (xsm > 48 * 1024)
+                KMC_CUDA_TRY(cudaFuncSetAttribute(xk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)xsm));
+            const int64_t xg = std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)num_sms() * 8));
+            xk<<<(unsigned)xg, kXImageThreads, xsm, s>>>(p.X, p.n, p.d, d4, nkb, ntiles, consts,
+                                                         ximg, xrow, nx, ndx);
+        }
         KMC_TRY(check_launch("x_image"));
         this->launches += 3;
         return KMC_OK;
