@@ -426,6 +426,36 @@ int kmc_fit_create_f64_i64(const double *X_t, const double *sample_weight, doubl
                            int64_t *assignment_id, double *res_centroids_t, int64_t n_samples,
                            int64_t n_features, int64_t n_clusters, double tol, int64_t max_iter,
                            int form, kmc_stream_t stream, kmc_fit_t *fit_out);
+/* Row-major input.  No counterpart in the reference, whose entry points take
+ * feature-major X_t (n_features, n_samples) only: the same fit session for X
+ * given as (n_samples, n_features) C-contiguous, other arguments as above.
+ * The mixed forms read it directly in their one-time operand conversion (no
+ * transposed copy is made); the plain form makes one feature-major copy on
+ * the device. */
+int kmc_fit_create_rowmajor_f32_i32(const float *X, const float *sample_weight,
+                                    float *centroids_t, int32_t *assignment_id,
+                                    float *res_centroids_t, int64_t n_samples,
+                                    int64_t n_features, int64_t n_clusters, double tol,
+                                    int64_t max_iter, int form, kmc_stream_t stream,
+                                    kmc_fit_t *fit_out);
+int kmc_fit_create_rowmajor_f32_i64(const float *X, const float *sample_weight,
+                                    float *centroids_t, int64_t *assignment_id,
+                                    float *res_centroids_t, int64_t n_samples,
+                                    int64_t n_features, int64_t n_clusters, double tol,
+                                    int64_t max_iter, int form, kmc_stream_t stream,
+                                    kmc_fit_t *fit_out);
+int kmc_fit_create_rowmajor_f64_i32(const double *X, const double *sample_weight,
+                                    double *centroids_t, int32_t *assignment_id,
+                                    double *res_centroids_t, int64_t n_samples,
+                                    int64_t n_features, int64_t n_clusters, double tol,
+                                    int64_t max_iter, int form, kmc_stream_t stream,
+                                    kmc_fit_t *fit_out);
+int kmc_fit_create_rowmajor_f64_i64(const double *X, const double *sample_weight,
+                                    double *centroids_t, int64_t *assignment_id,
+                                    double *res_centroids_t, int64_t n_samples,
+                                    int64_t n_features, int64_t n_clusters, double tol,
+                                    int64_t max_iter, int form, kmc_stream_t stream,
+                                    kmc_fit_t *fit_out);
 /* Enqueue n_iterations iterations (asynchronous; no-ops once the loop stopped). */
 int kmc_fit_step(kmc_fit_t fit, int64_t n_iterations);
 /* Run to convergence (blocking). */

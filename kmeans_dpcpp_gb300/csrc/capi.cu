@@ -269,7 +269,8 @@ int driver(const T *X, const T *w, T *init_c, I *labels, T *res_c, int64_t n, in
 
 template <typename T, typename I>
 int fit_create(const T *X, const T *w, T *c, I *labels, T *rc, int64_t n, int64_t d, int64_t k,
-               double tol, int64_t max_iter, int form, cudaStream_t s, FitBase **out) {
+               double tol, int64_t max_iter, int form, cudaStream_t s, FitBase **out,
+               int rowmajor = 0) {
     CHECK_DIMS(n, d, k, max_iter);
     KMC_CHECK_ARG(out != nullptr, "null output pointer");
     KMC_CHECK_ARG(k > 0, "n_clusters must be positive");
@@ -286,6 +287,7 @@ int fit_create(const T *X, const T *w, T *c, I *labels, T *rc, int64_t n, int64_
     p.tol = tol;
     p.max_iter = max_iter;
     p.stream = s;
+    p.x_rowmajor = rowmajor;
     std::unique_ptr<FitBase> fit;
     KMC_TRY(make_fit<T, I>(p, form, &fit));
     *out = fit.release();
@@ -408,6 +410,21 @@ KMC_FIT_CREATE(f32_i32, float, int32_t)
 KMC_FIT_CREATE(f32_i64, float, int64_t)
 KMC_FIT_CREATE(f64_i32, double, int32_t)
 KMC_FIT_CREATE(f64_i64, double, int64_t)
+
+#define KMC_FIT_CREATE_ROWMAJOR(SUF, T, I)                                                    \
+    int kmc_fit_create_rowmajor_##SUF(const T *X, const T *w, T *c, I *lab, T *rc, int64_t n,  \
+                                      int64_t d, int64_t k, double tol, int64_t max_iter,      \
+                                      int form, kmc_stream_t s, kmc_fit_t *out) {              \
+        KMC_CHECK_ARG(out != nullptr, "null output pointer");                                  \
+        FitBase *f = nullptr;                                                                  \
+        KMC_TRY(fit_create<T, I>(X, w, c, lab, rc, n, d, k, tol, max_iter, form, S(s), &f, 1)); \
+        *out = new kmc_fit_s{f};                                                               \
+        return KMC_OK;                                                                         \
+    }
+KMC_FIT_CREATE_ROWMAJOR(f32_i32, float, int32_t)
+KMC_FIT_CREATE_ROWMAJOR(f32_i64, float, int64_t)
+KMC_FIT_CREATE_ROWMAJOR(f64_i32, double, int32_t)
+KMC_FIT_CREATE_ROWMAJOR(f64_i64, double, int64_t)
 
 #define KMC_FIT_CHECK(fit) KMC_CHECK_ARG((fit) != nullptr && (fit)->impl != nullptr, "null fit")
 

@@ -57,6 +57,17 @@ int PlainFit<T, I>::init(const FitParams<T, I> &p) {
     const size_t o_tsc = take(threshold_scratch_bytes());
     const size_t o_ssc = take(select_scratch_bytes(k));
     KMC_TRY(ws.alloc(off, p.stream));
+    if (p.x_rowmajor && !reads_rowmajor()) {
+        KMC_TRY(xt.alloc(sizeof(T) * (size_t)n * (size_t)d, p.stream));
+        if (sizeof(T) == 4)
+            KMC_TRY(kmc_transpose_f32(reinterpret_cast<const float *>(p.X), xt.as<float>(), n, d,
+                                      reinterpret_cast<kmc_stream_t>(p.stream)));
+        else
+            KMC_TRY(kmc_transpose_f64(reinterpret_cast<const double *>(p.X), xt.as<double>(), n,
+                                      d, reinterpret_cast<kmc_stream_t>(p.stream)));
+        prm.X = xt.as<T>();
+        prm.x_rowmajor = 0;
+    }
     char *b = ws.as<char>();
     state = reinterpret_cast<LoopState *>(b + o_state);
     hn = reinterpret_cast<T *>(b + o_hn);
@@ -98,6 +109,9 @@ int PlainFit<T, I>::enqueue_iteration() {
     T *cur = p.centroids;       // this_centroids_t
     T *nxt = p.new_centroids;   // new_centroids_t
     const int64_t thr_launches = 1 + 2 * (sizeof(T) == 4 ? 4 : 8);
+    const T *xv = nullptr;
+    int64_t xfs = 0, xss = 0;
+    x_view(&xv, &xfs, &xss);
     // kmeans_lloyd_driver.hpp:86-111
     KMC_TRY(launch_half_norm<T>(cur, hn, d, k, s, state));
     KMC_TRY(launch_fill<double>(sums_cp, 0.0, P * d * k, s, state));
@@ -121,20 +135,22 @@ int PlainFit<T, I>::enqueue_iteration() {
     int64_t verbose_launches = 0;
     if (p.verbose) {
         // kmeans_lloyd_driver.hpp:179-197: inertia of the *undivided* sums.
-        KMC_TRY(launch_inertia<T, I>(p.X, p.w, nxt, p.labels, sq_dist, n, d, k, s, state));
+        KMC_TRY(launch_inertia<T, I>(xv, p.w, nxt, p.labels, sq_dist, n, d, k, s, state, nullptr,
+                                     xfs, xss));
         KMC_TRY(launch_sum_f64<T>(sq_dist, n, partials, dsum, s, state));
         verbose_launches = 3;
     }
     // kmeans_lloyd_driver.hpp:217-312, gated on the device value of n_empty.
     KMC_TRY(launch_gate_from_count<I>(n_empty, gate, s, state));
-    KMC_TRY(launch_inertia<T, I>(p.X, nullptr, cur, p.labels, sq_dist, n, d, k, s, state, gate));
+    KMC_TRY(launch_inertia<T, I>(xv, nullptr, cur, p.labels, sq_dist, n, d, k, s, state, gate,
+                                 xfs, xss));
     KMC_TRY(launch_threshold<T>(sq_dist, n, gate, 0, threshold, thr_scratch, s, state));
     KMC_TRY(launch_fill<I>(counters, I(0), 1, s, state));
     KMC_TRY(launch_fill<I>(counters + 1, I(1), 1, s, state));
     KMC_TRY(launch_select<T, I>(gate, 0, sq_dist, threshold, selected, counters, counters + 1, n,
                                 sel_scratch, s, state));
-    KMC_TRY(launch_relocate<T, I>(gate, 0, p.X, p.w, p.labels, selected, counters, empty_list,
-                                  nxt, sizes, sq_dist, n, d, k, s, state));
+    KMC_TRY(launch_relocate<T, I>(gate, 0, xv, p.w, p.labels, selected, counters, empty_list,
+                                  nxt, sizes, sq_dist, n, d, k, s, state, xfs, xss));
     // kmeans_lloyd_driver.hpp:317-353
     KMC_TRY(launch_divide_and_shift<T>(cur, nxt, sizes, shifts, d, k, s, state));
     KMC_TRY(launch_loop_control<T>(shifts, k, state, s));
@@ -199,7 +215,11 @@ int PlainFit<T, I>::finalize(int64_t *n_iter_out, double *inertia_out) {
     // the final centroids.
     KMC_TRY(launch_half_norm<T>(p.centroids, hn, d, k, s));
     KMC_TRY(final_assignment());
-    KMC_TRY(launch_inertia<T, I>(p.X, p.w, p.centroids, p.labels, sq_dist, n, d, k, s));
+    const T *xv = nullptr;
+    int64_t xfs = 0, xss = 0;
+    x_view(&xv, &xfs, &xss);
+    KMC_TRY(launch_inertia<T, I>(xv, p.w, p.centroids, p.labels, sq_dist, n, d, k, s, nullptr,
+                                 nullptr, xfs, xss));
     KMC_TRY(launch_sum_f64<T>(sq_dist, n, partials, dsum, s));
     launches += 5;
     if (p.new_centroids != p.centroids && d * k > 0)

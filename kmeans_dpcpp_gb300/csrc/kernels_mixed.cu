@@ -666,7 +666,8 @@ __device__ __forceinline__ float round16(float v) {
 
 // One CTA per 128-sample tile (including the zero rows that pad the last
 // tile): the tile's features are staged in shared memory (coalesced reads of
-// each feature's 128 samples), then written out as the 128-byte-swizzled
+// each feature's 128 samples from a feature-major X, or of each sample's d
+// features from a row-major one), then written out as the 128-byte-swizzled
 // K-major image of (x * sigma) and the row-major fp32 copy of x (features
 // d..d4-1 zero), both as contiguous 16-byte chunks, and per sample ||x|| and
 // the norm of the image's rounding error ||round16(x sigma) - x sigma|| /
@@ -681,17 +682,26 @@ __host__ __device__ inline size_t x_image_smem(int nkb) {
 template <int BF16>
 __global__ void __launch_bounds__(kXImageThreads) x_image_kernel(
     const float *X, int64_t n, int64_t d, int64_t d4, int nkb, int64_t ntiles,
-    const MixedConsts *c, uint8_t *img, float *xrow, float *nx, float *ndx) {
+    const MixedConsts *c, uint8_t *img, float *xrow, float *nx, float *ndx, int rowmajor) {
     extern __shared__ float xs[];  // [feature][kXsPitch]
     const float sigma = c->sigma;
     const int F = nkb * 64;
     const int g4 = (int)(d4 / 4);
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t i0 = tile * kTileM;
-        for (int e = threadIdx.x; e < F * kTileM; e += kXImageThreads) {
-            const int f = e >> 7, r = e & (kTileM - 1);
-            const int64_t i = i0 + r;
-            xs[f * kXsPitch + r] = (f < d && i < n) ? X[(int64_t)f * n + i] : 0.f;
+        if (rowmajor) {
+            const int fshift = (nkb == 2) ? 7 : 6;  // F = 64 nkb
+            for (int e = threadIdx.x; e < F * kTileM; e += kXImageThreads) {
+                const int r = e >> fshift, f = e & (F - 1);
+                const int64_t i = i0 + r;
+                xs[f * kXsPitch + r] = (f < d && i < n) ? X[i * d + f] : 0.f;
+            }
+        } else {
+            for (int e = threadIdx.x; e < F * kTileM; e += kXImageThreads) {
+                const int f = e >> 7, r = e & (kTileM - 1);
+                const int64_t i = i0 + r;
+                xs[f * kXsPitch + r] = (f < d && i < n) ? X[(int64_t)f * n + i] : 0.f;
+            }
         }
         __syncthreads();
         // image: 16-byte chunk q of feature block kb holds row r, features
@@ -1128,6 +1138,15 @@ struct MixedFit : PlainFit<float, I> {
     int *flagged = nullptr, *n_flagged = nullptr, *err_dev = nullptr;
     long long *stats = nullptr;  // [0] last pass, [1] total
 
+    // The one-time conversion reads X in either layout; afterwards every
+    // kernel reads the row-major fp32 copy.
+    bool reads_rowmajor() const override { return true; }
+    void x_view(const float **x, int64_t *fs, int64_t *ss) const override {
+        *x = xrow;
+        *fs = 1;
+        *ss = d4;
+    }
+
     static bool supported(int64_t d, int64_t k) {
         const int nk = (int)ceil_div<int64_t>(std::max<int64_t>(d, 1), 64);
         const int64_t kp = ceil_div<int64_t>(std::max<int64_t>(k, 1), kChunkN) * kChunkN;
@@ -1223,7 +1242,7 @@ struct MixedFit : PlainFit<float, I> {
                                                   (int)xsm));
             const int64_t xg = std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)num_sms() * 8));
             xk<<<(unsigned)xg, kXImageThreads, xsm, s>>>(p.X, p.n, p.d, d4, nkb, ntiles, consts,
-                                                         ximg, xrow, nx, ndx);
+                                                         ximg, xrow, nx, ndx, p.x_rowmajor);
         }
         KMC_TRY(check_launch("x_image"));
         this->launches += 3;

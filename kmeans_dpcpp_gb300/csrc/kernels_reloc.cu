@@ -334,7 +334,8 @@ template <typename T, typename I>
 __global__ void relocate_kernel(const int64_t *n_empty_dev, int64_t n_empty_host, const T *X,
                                 const T *w, const I *labels, const I *selected, const I *n_gt,
                                 const I *empty_list, T *sums, T *sizes, T *inertia, int64_t n,
-                                int64_t d, int64_t k, const LoopState *guard) {
+                                int64_t d, int64_t k, const LoopState *guard, int64_t fs,
+                                int64_t ss) {
     if (stopped(guard)) return;
     int64_t n_empty = (n_empty_dev != nullptr) ? *n_empty_dev : n_empty_host;
     if (n_empty <= 0) return;
@@ -353,7 +354,7 @@ __global__ void relocate_kernel(const int64_t *n_empty_dev, int64_t n_empty_host
         // caller-supplied indices: never dereference out of range
         if (old < 0 || old >= k || cl < 0 || cl >= k) continue;
         T wv = w[s];
-        T xw = mul_rn(X[f * n + s], wv);  // rounded product, as in the reference
+        T xw = mul_rn(X[f * fs + s * ss], wv);  // rounded product, as in the reference
         sums[f * k + old] -= xw;
         sums[f * k + cl] = xw;
         if (f == 0) {
@@ -416,11 +417,13 @@ template <typename T, typename I>
 int launch_relocate(const int64_t *n_empty_dev, int64_t n_empty_host, const T *X, const T *w,
                     const I *labels, const I *selected, const I *n_gt, const I *empty_list,
                     T *sums, T *sizes, T *inertia, int64_t n, int64_t d, int64_t k,
-                    cudaStream_t s, const LoopState *guard) {
+                    cudaStream_t s, const LoopState *guard, int64_t x_fstride,
+                    int64_t x_sstride) {
     int grid = (int)ceil_div<int64_t>(std::max<int64_t>(d, 1), 128);
+    const int64_t fs = x_fstride > 0 ? x_fstride : n, ss = x_fstride > 0 ? x_sstride : 1;
     relocate_kernel<T, I><<<grid, 128, 0, s>>>(n_empty_dev, n_empty_host, X, w, labels, selected,
                                                n_gt, empty_list, sums, sizes, inertia, n, d, k,
-                                               guard);
+                                               guard, fs, ss);
     return check_launch("relocate");
 }
 
@@ -441,7 +444,7 @@ template int launch_threshold<double>(const double *, int64_t, const int64_t *, 
     template int launch_relocate<T, I>(const int64_t *, int64_t, const T *, const T *,        \
                                        const I *, const I *, const I *, const I *, T *, T *,  \
                                        T *, int64_t, int64_t, int64_t, cudaStream_t,          \
-                                       const LoopState *);
+                                       const LoopState *, int64_t, int64_t);
 KMC_INST_RELOC(float, int32_t)
 KMC_INST_RELOC(float, int64_t)
 KMC_INST_RELOC(double, int32_t)

@@ -195,7 +195,7 @@ __global__ void loop_control_kernel(const T *shifts, int64_t k, LoopState *st) {
 template <typename T, typename I>
 __global__ void inertia_kernel(const T *X, const T *w, const T *C, const I *labels, T *out,
                                int64_t n, int64_t d, int64_t k, const LoopState *guard,
-                               const int64_t *gate) {
+                               const int64_t *gate, int64_t fs, int64_t ss) {
     if (stopped(guard)) return;
     if (gate != nullptr && *gate == 0) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -207,7 +207,7 @@ __global__ void inertia_kernel(const T *X, const T *w, const T *C, const I *labe
         }
         T acc = T(0);
         for (int64_t f = 0; f < d; ++f) {
-            T diff = X[f * n + i] - C[f * k + c];
+            T diff = X[f * fs + i * ss] - C[f * k + c];
             acc = fma_t(diff, diff, acc);
         }
         out[i] = (w != nullptr) ? mul_rn(acc, w[i]) : acc;
@@ -318,10 +318,11 @@ int launch_loop_control(const T *shifts, int64_t k, LoopState *state, cudaStream
 template <typename T, typename I>
 int launch_inertia(const T *X, const T *w, const T *C, const I *labels, T *out, int64_t n,
                    int64_t d, int64_t k, cudaStream_t s, const LoopState *guard,
-                   const int64_t *gate) {
+                   const int64_t *gate, int64_t x_fstride, int64_t x_sstride) {
     if (n == 0) return KMC_OK;
+    const int64_t fs = x_fstride > 0 ? x_fstride : n, ss = x_fstride > 0 ? x_sstride : 1;
     inertia_kernel<T, I><<<grid_for(n, 256, 16384), 256, 0, s>>>(X, w, C, labels, out, n, d, k,
-                                                                 guard, gate);
+                                                                 guard, gate, fs, ss);
     return check_launch("compute_inertia");
 }
 
@@ -363,7 +364,7 @@ int launch_fill(T *p, T v, int64_t count, cudaStream_t s, const LoopState *guard
                                          const LoopState *);                                  \
     template int launch_inertia<T, I>(const T *, const T *, const T *, const I *, T *,        \
                                       int64_t, int64_t, int64_t, cudaStream_t,                \
-                                      const LoopState *, const int64_t *);
+                                      const LoopState *, const int64_t *, int64_t, int64_t);
 
 KMC_INST_T(float)
 KMC_INST_T(double)

@@ -11,7 +11,7 @@ namespace kmc {
 
 template <typename T, typename I>
 struct FitParams {
-    const T *X = nullptr;         // (d, n) feature-major samples
+    const T *X = nullptr;         // (d, n) feature-major samples, or (n, d) if x_rowmajor
     const T *w = nullptr;         // (n,) sample weights
     T *centroids = nullptr;       // (d, k) current centroids; overwritten
     T *new_centroids = nullptr;   // (d, k) result buffer
@@ -23,6 +23,7 @@ struct FitParams {
     kmc_print_fn print_fn = nullptr;
     void *print_ctx = nullptr;
     cudaStream_t stream = nullptr;
+    int x_rowmajor = 0;           // X given as (n, d) C-contiguous
 };
 
 struct FitBase {
@@ -80,6 +81,7 @@ struct PlainFit : FitBase {
     void *thr_scratch = nullptr, *sel_scratch = nullptr;
     int64_t issued = 0;
     int host_done = 0;
+    Scratch xt;  // feature-major copy of a row-major X (forms that need one)
 
     int init(const FitParams<T, I> &p);
     int enqueue_iteration() override;
@@ -94,6 +96,16 @@ struct PlainFit : FitBase {
     // Private copies -> new centroid sums, sizes and the empty-cluster list
     // (kmeans_lloyd_driver.hpp:155-170).
     virtual int reduce_step(T *nxt);
+    // Whether the form reads a row-major X itself (else init makes a
+    // feature-major copy).
+    virtual bool reads_rowmajor() const { return false; }
+    // The samples as the inertia and relocation kernels read them: element
+    // (f, i) at x[f * fs + i * ss].
+    virtual void x_view(const T **x, int64_t *fs, int64_t *ss) const {
+        *x = prm.X;
+        *fs = prm.n;
+        *ss = 1;
+    }
 };
 
 // Mixed tensor-core form (kernels_mixed.cu); float32 data only.

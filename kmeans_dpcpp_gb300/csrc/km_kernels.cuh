@@ -47,11 +47,13 @@ int launch_divide_and_shift(const T *old_c, T *new_c, const T *sizes, T *shifts,
 // Loop control: float64 total of shifts, n_iter += 1, convergence test.
 template <typename T>
 int launch_loop_control(const T *shifts, int64_t k, LoopState *state, cudaStream_t s);
-// w == nullptr selects the unit-weight variant.
+// w == nullptr selects the unit-weight variant.  X is feature-major (d, n)
+// unless x_fstride > 0: then element (f, i) is X[f * x_fstride + i * x_sstride]
+// (a row-major copy has x_fstride = 1, x_sstride = its row length).
 template <typename T, typename I>
 int launch_inertia(const T *X, const T *w, const T *C, const I *labels, T *out, int64_t n,
                    int64_t d, int64_t k, cudaStream_t s, const LoopState *guard = nullptr,
-                   const int64_t *gate = nullptr);
+                   const int64_t *gate = nullptr, int64_t x_fstride = 0, int64_t x_sstride = 1);
 // Deterministic float64 sum of n values into *out (device).  `partials` must
 // hold sum_partials_size() doubles.
 int64_t sum_partials_size();
@@ -92,7 +94,8 @@ template <typename T, typename I>
 int launch_relocate(const int64_t *n_empty_dev, int64_t n_empty_host, const T *X, const T *w,
                     const I *labels, const I *selected, const I *n_gt, const I *empty_list,
                     T *sums, T *sizes, T *inertia, int64_t n, int64_t d, int64_t k,
-                    cudaStream_t s, const LoopState *guard = nullptr);
+                    cudaStream_t s, const LoopState *guard = nullptr, int64_t x_fstride = 0,
+                    int64_t x_sstride = 1);
 // Copies *n_empty (indT) into an int64 device scalar (0 when the loop stopped).
 template <typename I>
 int launch_gate_from_count(const I *n_empty, int64_t *gate, cudaStream_t s,
