@@ -530,6 +530,14 @@ int kmc_batch_add_fit_f32(kmc_batch_t batch, const float *X_t, const float *samp
 int kmc_batch_add_predict_f32(kmc_batch_t batch, const float *X_t, const float *centroids_t,
                               int32_t *labels, int64_t n_samples, int64_t n_features,
                               int64_t n_clusters, int64_t *instance_out);
+/* Batched transform: the (n_clusters, n_samples) Euclidean distances of
+ * compute_centroid_to_sample_distances (compute_euclidean_distance.hpp:
+ * 12-114, the intended full result) into `distances`, computed in the next
+ * engine step by the same persistent tiles as the assignments (bit-equal to
+ * kmc_compute_centroid_to_sample_distances_f32). */
+int kmc_batch_add_transform_f32(kmc_batch_t batch, const float *X_t, const float *centroids_t,
+                                float *distances, int64_t n_samples, int64_t n_features,
+                                int64_t n_clusters, int64_t *instance_out);
 /* One engine step; *n_active_out = instances still running afterwards. */
 int kmc_batch_step(kmc_batch_t batch, int64_t *n_active_out);
 /* Steps until every instance has finished. */
@@ -563,7 +571,7 @@ int kmc_seeded_rows(int64_t n_samples, int64_t n_clusters, uint64_t seed, int32_
  * seconds from the start of the replay. */
 typedef struct {
     double arrival_s;
-    int32_t kind;        /* 0 fit, 1 predict */
+    int32_t kind;        /* 0 fit, 1 predict, 2 transform (distances; result.inertia = their float64 sum) */
     int32_t n_features;
     int64_t n_samples;
     int64_t n_clusters;
@@ -571,7 +579,7 @@ typedef struct {
     uint64_t seed;
     double tol;
     int64_t max_iter;
-    int64_t model;       /* predict: index of the fit request whose centroids it uses */
+    int64_t model;       /* predict, transform: index of the fit request whose centroids it uses */
     float std_lo, std_hi;
 } kmc_serve_request_t;
 typedef struct {

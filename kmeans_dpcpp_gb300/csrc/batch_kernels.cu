@@ -58,7 +58,7 @@ __device__ double block_sum_b(double v, double *sh) {
 }
 
 __global__ void batch_prep_kernel(BInst *tab, const int *idx, int count, int *counters) {
-    if (blockIdx.x == 0 && threadIdx.x < kBatchVariants) counters[threadIdx.x] = 0;
+    if (blockIdx.x == 0 && threadIdx.x < 2 * kBatchVariants) counters[threadIdx.x] = 0;
     if ((int)blockIdx.x >= count) return;
     BInst &in = tab[idx[blockIdx.x]];
     const int d = in.d, k = in.k;
@@ -102,7 +102,10 @@ struct BTile {
         sizeof(float) * (2 * kBK * BM + 2 * kBK * BN + BN + BM) + sizeof(long long) * BM;
 };
 
-template <int TN>
+// DIST = 1: the items are B_TRANSFORM instances, whose (k, n) Euclidean
+// distances sqrt(sum_f (c - x)^2) are written instead of labels (the plain
+// form's MODE_DIST arithmetic, compute_euclidean_distance.hpp:12-114).
+template <int TN, int DIST>
 __global__ void __launch_bounds__(kThreadsB, 2)
     batch_assign_kernel(const BInst *tab, const BItem *items, int n_items, int *counter) {
     using G = BTile<TN>;
@@ -201,10 +204,31 @@ __global__ void __launch_bounds__(kThreadsB, 2)
 #pragma unroll
                         for (int m = 0; m < kTM; ++m)
 #pragma unroll
-                            for (int q = 0; q < TN; ++q) acc[m][q] = __fmaf_rn(xv[m], cv[q], acc[m][q]);
+                            for (int q = 0; q < TN; ++q) {
+                                if (DIST) {
+                                    const float diff = cv[q] - xv[m];
+                                    acc[m][q] = __fmaf_rn(diff, diff, acc[m][q]);
+                                } else {
+                                    acc[m][q] = __fmaf_rn(xv[m], cv[q], acc[m][q]);
+                                }
+                            }
                     }
                     if (ch + 1 < nchunks) store_smem(buf ^ 1);
                     __syncthreads();
+                }
+                if (DIST) {
+#pragma unroll
+                    for (int m = 0; m < kTM; ++m) {
+                        const int s = (m < HM) ? ty * HM + m : BM / 2 + ty * HM + (m - HM);
+                        const int64_t i = i0 + s;
+#pragma unroll
+                        for (int q = 0; q < TN; ++q) {
+                            const int cl = (q < HN) ? tx * HN + q : BN / 2 + tx * HN + (q - HN);
+                            const int j = c0 + cl;
+                            if (i < n && j < k) in.dist[(int64_t)j * n + i] = __fsqrt_rn(acc[m][q]);
+                        }
+                    }
+                    continue;  // smem buffers are rewritten only after the next step's barrier
                 }
                 // ascending centroid order within this thread's columns
 #pragma unroll
@@ -223,6 +247,7 @@ __global__ void __launch_bounds__(kThreadsB, 2)
                 }
                 __syncthreads();
             }
+            if (DIST) continue;
             // (value, index) minimum over the 16 threads sharing these samples
 #pragma unroll
             for (int m = 0; m < kTM; ++m) {
@@ -406,18 +431,18 @@ struct AssignShape {
     int grid = 0;
 };
 std::mutex g_shape_mu;
-AssignShape g_shape[kBatchVariants][64];  // [variant][device]
+AssignShape g_shape[2][kBatchVariants][64];  // [dist][variant][device]
 
-template <int TN>
+template <int TN, int DIST>
 int assign_shape(int variant, AssignShape *out) {
     int dev = 0;
     KMC_CUDA_TRY(cudaGetDevice(&dev));
     KMC_CHECK_ARG(dev >= 0 && dev < 64, "device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_shape_mu);
-    AssignShape &sh = g_shape[variant][dev];
+    AssignShape &sh = g_shape[DIST][variant][dev];
     if (sh.grid == 0) {
         const size_t smem = BTile<TN>::base_bytes + kPrivBytes;
-        auto kern = batch_assign_kernel<TN>;
+        auto kern = batch_assign_kernel<TN, DIST>;
         KMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem));
         int per_sm = 0;
@@ -430,15 +455,15 @@ int assign_shape(int variant, AssignShape *out) {
     return KMC_OK;
 }
 
-template <int TN>
+template <int TN, int DIST>
 int launch_assign_v(int variant, const BInst *tab, const BItem *items, int n_items,
                     int *counter, cudaStream_t s) {
     AssignShape sh;
-    KMC_TRY(assign_shape<TN>(variant, &sh));
+    KMC_TRY((assign_shape<TN, DIST>(variant, &sh)));
     int grid = sh.grid;
     if (grid > n_items) grid = n_items;
     if (grid < 1) return KMC_OK;
-    batch_assign_kernel<TN><<<grid, kThreadsB, sh.smem, s>>>(tab, items, n_items, counter);
+    batch_assign_kernel<TN, DIST><<<grid, kThreadsB, sh.smem, s>>>(tab, items, n_items, counter);
     return check_launch("batch_assign");
 }
 
@@ -505,17 +530,25 @@ int launch_batch_prep(BInst *tab, const int *idx, int count, int *counters, cuda
 
 int prepare_batch_assign() {
     AssignShape sh;
-    KMC_TRY(assign_shape<2>(0, &sh));
-    KMC_TRY(assign_shape<4>(1, &sh));
-    return assign_shape<8>(2, &sh);
+    KMC_TRY((assign_shape<2, 0>(0, &sh)));
+    KMC_TRY((assign_shape<4, 0>(1, &sh)));
+    KMC_TRY((assign_shape<8, 0>(2, &sh)));
+    KMC_TRY((assign_shape<2, 1>(0, &sh)));
+    KMC_TRY((assign_shape<4, 1>(1, &sh)));
+    return assign_shape<8, 1>(2, &sh);
 }
 
-int launch_batch_assign(int variant, const BInst *tab, const BItem *items, int n_items,
-                        int *counter, cudaStream_t s) {
+int launch_batch_assign(int variant, int dist, const BInst *tab, const BItem *items,
+                        int n_items, int *counter, cudaStream_t s) {
     if (n_items <= 0) return KMC_OK;
-    if (variant == 0) return launch_assign_v<2>(0, tab, items, n_items, counter, s);
-    if (variant == 1) return launch_assign_v<4>(1, tab, items, n_items, counter, s);
-    return launch_assign_v<8>(2, tab, items, n_items, counter, s);
+    if (dist) {
+        if (variant == 0) return launch_assign_v<2, 1>(0, tab, items, n_items, counter, s);
+        if (variant == 1) return launch_assign_v<4, 1>(1, tab, items, n_items, counter, s);
+        return launch_assign_v<8, 1>(2, tab, items, n_items, counter, s);
+    }
+    if (variant == 0) return launch_assign_v<2, 0>(0, tab, items, n_items, counter, s);
+    if (variant == 1) return launch_assign_v<4, 0>(1, tab, items, n_items, counter, s);
+    return launch_assign_v<8, 0>(2, tab, items, n_items, counter, s);
 }
 
 int launch_batch_reduce(BInst *tab, const int *idx, int count, int *n_empty_out,
@@ -630,7 +663,7 @@ int tune_variant(int64_t d, int64_t k_in, cudaStream_t s, int *variant) {
         for (int rep = 0; rep < 3; ++rep) {
             KMC_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int), s));
             KMC_CUDA_TRY(cudaEventRecord(e0, s));
-            KMC_TRY(launch_batch_assign(v, tab, items, 64, cnt, s));
+            KMC_TRY(launch_batch_assign(v, 0, tab, items, 64, cnt, s));
             KMC_CUDA_TRY(cudaEventRecord(e1, s));
             KMC_CUDA_TRY(cudaEventSynchronize(e1));
             float ms = 0.f;

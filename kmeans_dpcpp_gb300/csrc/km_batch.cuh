@@ -12,7 +12,7 @@
 
 namespace kmc {
 
-enum BatchMode : int { B_FIT = 0, B_ASSIGN = 1 };
+enum BatchMode : int { B_FIT = 0, B_ASSIGN = 1, B_TRANSFORM = 2 };
 
 // Device table entry of one instance.  X, w, C and labels are the caller's
 // arrays (C is the caller's initial-centroid buffer and is overwritten, as in
@@ -26,6 +26,7 @@ struct BInst {
     float *sizes;          // (k,) float32 cluster sizes
     double *sums;          // (d*k + k,) float64 sums (f*k + j), then sizes
     int32_t *labels;       // (n,)
+    float *dist;           // (k, n) distances (B_TRANSFORM)
     int32_t *empty_list;   // (k + 1,) ascending list, count at [k]
     long long n;
     int d, k;
@@ -52,8 +53,9 @@ size_t batch_assign_smem(int v);
 int launch_batch_prep(BInst *tab, const int *idx, int count, int *counters, cudaStream_t s);
 // Sets the assign kernels' shared-memory attributes (outside graph capture).
 int prepare_batch_assign();
-int launch_batch_assign(int variant, const BInst *tab, const BItem *items, int n_items,
-                        int *counter, cudaStream_t s);
+// dist != 0: the transform kernel (items of B_TRANSFORM instances only).
+int launch_batch_assign(int variant, int dist, const BInst *tab, const BItem *items,
+                        int n_items, int *counter, cudaStream_t s);
 int launch_batch_reduce(BInst *tab, const int *idx, int count, int *n_empty_out,
                         cudaStream_t s);
 int launch_batch_update(BInst *tab, const int *idx, int count, int *done_out, cudaStream_t s);

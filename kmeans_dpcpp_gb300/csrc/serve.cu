@@ -117,8 +117,9 @@ struct BatchEngine {
     std::vector<double> res_inertia;
     // current step plan
     std::vector<int> all, fits;
-    int n_items[kBatchVariants] = {0, 0, 0};
-    int64_t item_off[kBatchVariants] = {0, 0, 0};
+    // [0][v]: assignment items of variant v, [1][v]: transform items
+    int n_items[2][kBatchVariants] = {{0, 0, 0}, {0, 0, 0}};
+    int64_t item_off[2][kBatchVariants] = {{0, 0, 0}, {0, 0, 0}};
     bool dirty = true;
     GraphExec gA, gB;
     int *host_i = nullptr;  // pinned: empty counts then done flags
@@ -162,7 +163,7 @@ struct BatchEngine {
         const size_t o_all = o_tab + align256(sizeof(BInst) * cap);
         const size_t o_fit = o_all + align256(sizeof(int) * cap);
         const size_t o_cnt = o_fit + align256(sizeof(int) * cap);
-        const size_t o_ne = o_cnt + align256(sizeof(int) * kBatchVariants);
+        const size_t o_ne = o_cnt + align256(sizeof(int) * 2 * kBatchVariants);
         const size_t o_dn = o_ne + align256(sizeof(int) * cap);
         KMC_TRY(dev.alloc(o_dn + align256(sizeof(int) * cap), s));
         char *b = dev.as<char>();
@@ -200,12 +201,13 @@ struct BatchEngine {
     }
 
     int add(int mode, const float *X, const float *w, float *C, int32_t *labels, int64_t n,
-            int64_t d, int64_t k, double tol, int64_t max_iter, int64_t *out) {
+            int64_t d, int64_t k, double tol, int64_t max_iter, int64_t *out,
+            float *dist = nullptr) {
         KMC_CHECK_ARG(n >= 0 && d >= 1 && k >= 1, "invalid dimensions (n=%lld, d=%lld, k=%lld)",
                       (long long)n, (long long)d, (long long)k);
         KMC_CHECK_ARG(d <= 1024 && k <= 4096, "batched fits take d <= 1024 and k <= 4096");
         KMC_CHECK_ARG(n < (int64_t(1) << 31), "n_samples must fit int32 labels");
-        KMC_CHECK_ARG(mode == B_ASSIGN || k <= n, "n_clusters exceeds n_samples");
+        KMC_CHECK_ARG(mode != B_FIT || k <= n, "n_clusters exceeds n_samples");
         KMC_CHECK_ARG(tol >= 0.0, "Tolerance must be non-negative");
         int64_t q = 0;
         KMC_TRY(free_slot(&q));
@@ -225,6 +227,7 @@ struct BatchEngine {
         h.sizes = m->sizes;
         h.sums = m->sums;
         h.labels = labels;
+        h.dist = dist;
         h.empty_list = m->empty_list;
         h.n = n;
         h.d = (int)d;
@@ -268,33 +271,37 @@ struct BatchEngine {
     int plan() {
         all.clear();
         fits.clear();
-        std::vector<BItem> items[kBatchVariants];
+        std::vector<BItem> items[2][kBatchVariants];
         for (int64_t q = 0; q < cap; ++q) {
             if (state[(size_t)q] != RUNNING) continue;
             const BInst &h = tab[(size_t)q];
             all.push_back((int)q);
             if (h.mode == B_FIT) fits.push_back((int)q);
             const int64_t tiles = ceil_div<int64_t>(h.n, kBatchTileM);
+            const int kind = (h.mode == B_TRANSFORM) ? 1 : 0;
             for (int64_t t = 0; t < tiles; t += kItemTiles)
-                items[h.variant].push_back(
+                items[kind][h.variant].push_back(
                     BItem{(int)q, (int)std::min<int64_t>(kItemTiles, tiles - t), (long long)t});
         }
         int64_t total = 0;
-        for (int v = 0; v < kBatchVariants; ++v) {
-            item_off[v] = total;
-            n_items[v] = (int)items[v].size();
-            total += n_items[v];
-        }
+        for (int kind = 0; kind < 2; ++kind)
+            for (int v = 0; v < kBatchVariants; ++v) {
+                item_off[kind][v] = total;
+                n_items[kind][v] = (int)items[kind][v].size();
+                total += n_items[kind][v];
+            }
         if (total > items_cap) {
             items_cap = std::max<int64_t>(total, 2 * items_cap);
             KMC_TRY(items_mem.alloc(sizeof(BItem) * (size_t)items_cap, s));
             items_d = items_mem.as<BItem>();
         }
-        for (int v = 0; v < kBatchVariants; ++v)
-            if (n_items[v] > 0)
-                KMC_CUDA_TRY(cudaMemcpyAsync(items_d + item_off[v], items[v].data(),
-                                             sizeof(BItem) * n_items[v], cudaMemcpyHostToDevice,
-                                             s));
+        for (int kind = 0; kind < 2; ++kind)
+            for (int v = 0; v < kBatchVariants; ++v)
+                if (n_items[kind][v] > 0)
+                    KMC_CUDA_TRY(cudaMemcpyAsync(items_d + item_off[kind][v],
+                                                 items[kind][v].data(),
+                                                 sizeof(BItem) * n_items[kind][v],
+                                                 cudaMemcpyHostToDevice, s));
         if (!all.empty())
             KMC_CUDA_TRY(cudaMemcpyAsync(all_d, all.data(), sizeof(int) * all.size(),
                                          cudaMemcpyHostToDevice, s));
@@ -307,11 +314,15 @@ struct BatchEngine {
         KMC_TRY(capture(&gA, [&]() -> int {
             KMC_TRY(launch_batch_prep(tab_d, all_d, (int)all.size(), counters_d, s));
             KMC_CUDA_TRY(cudaEventRecord(ev_fork, s));
+            // one branch per centroid-window variant: its assignment items,
+            // then its transform items
             for (int v = 0; v < kBatchVariants; ++v) {
-                if (n_items[v] == 0) continue;
+                if (n_items[0][v] + n_items[1][v] == 0) continue;
                 KMC_CUDA_TRY(cudaStreamWaitEvent(side[v], ev_fork, 0));
-                KMC_TRY(launch_batch_assign(v, tab_d, items_d + item_off[v], n_items[v],
-                                            counters_d + v, side[v]));
+                for (int kind = 0; kind < 2; ++kind)
+                    KMC_TRY(launch_batch_assign(v, kind, tab_d, items_d + item_off[kind][v],
+                                                n_items[kind][v],
+                                                counters_d + kind * kBatchVariants + v, side[v]));
                 KMC_CUDA_TRY(cudaEventRecord(ev_join[v], side[v]));
                 KMC_CUDA_TRY(cudaStreamWaitEvent(s, ev_join[v], 0));
             }
@@ -404,7 +415,7 @@ struct BatchEngine {
             for (size_t t = 0; t < nf; ++t)
                 if (host_i[cap + t]) KMC_TRY(finish_fit(fits[t]));
             for (int q : all)
-                if (tab[(size_t)q].mode == B_ASSIGN) {
+                if (tab[(size_t)q].mode != B_FIT) {
                     state[(size_t)q] = FINISHED;
                     res_iter[(size_t)q] = 0;
                     dirty = true;
@@ -428,7 +439,12 @@ int64_t request_bytes(int kind, int64_t n, int64_t d, int64_t k, int form) {
     const int64_t d4 = ceil_div<int64_t>(std::max<int64_t>(d, 1), 4) * 4;
     int64_t b = (int64_t)(align256(sizeof(float) * n * d) + align256(sizeof(float) * n) +
                           align256(sizeof(float) * d * k) + align256(sizeof(int32_t) * n));
-    if (form == KMC_FORM_PLAIN) {
+    if (kind == 2) {
+        // distances, their float64 checksum, and the engine's assignment-sized slot
+        b += (int64_t)(align256(sizeof(float) * n * k) +
+                       align256(sizeof(double) * (sum_partials_size() + 1)) +
+                       slot_bytes(B_ASSIGN, n, d, k));
+    } else if (form == KMC_FORM_PLAIN) {
         b += (int64_t)slot_bytes(kind == 0 ? B_FIT : B_ASSIGN, n, d, k);
     } else {
         // plain-fit workspace plus the tensor-core operands: fp16/bf16 image,
@@ -446,18 +462,35 @@ struct ReqMem {
     Scratch mem;
     float *X = nullptr, *w = nullptr, *C = nullptr, *Cres = nullptr;
     int32_t *labels = nullptr;
+    float *dist = nullptr;        // transform: (k, n) distances
+    double *partials = nullptr;   // transform: checksum scratch, then the sum
 };
 
-int alloc_request(ReqMem &m, int64_t n, int64_t d, int64_t k, cudaStream_t s) {
+int alloc_request(ReqMem &m, int64_t n, int64_t d, int64_t k, int kind, cudaStream_t s) {
     const size_t bX = align256(sizeof(float) * n * d), bw = align256(sizeof(float) * n),
                  bC = align256(sizeof(float) * d * k), bl = align256(sizeof(int32_t) * n);
-    KMC_TRY(m.mem.alloc(bX + bw + 2 * bC + bl, s));
+    const size_t bD = kind == 2 ? align256(sizeof(float) * n * k) : 0;
+    const size_t bP = kind == 2 ? align256(sizeof(double) * (sum_partials_size() + 1)) : 0;
+    KMC_TRY(m.mem.alloc(bX + bw + 2 * bC + bl + bD + bP, s));
     char *b = m.mem.as<char>();
     m.X = reinterpret_cast<float *>(b);
     m.w = reinterpret_cast<float *>(b + bX);
     m.C = reinterpret_cast<float *>(b + bX + bw);
     m.Cres = reinterpret_cast<float *>(b + bX + bw + bC);
     m.labels = reinterpret_cast<int32_t *>(b + bX + bw + 2 * bC);
+    if (kind == 2) {
+        m.dist = reinterpret_cast<float *>(b + bX + bw + 2 * bC + bl);
+        m.partials = reinterpret_cast<double *>(b + bX + bw + 2 * bC + bl + bD);
+    }
+    return KMC_OK;
+}
+
+// Float64 total of a transform request's distances (deterministic order).
+int dist_checksum(ReqMem &m, int64_t n, int64_t k, cudaStream_t s, double *out) {
+    double *sum = m.partials + sum_partials_size();
+    KMC_TRY(launch_sum_f64<float>(m.dist, n * k, m.partials, sum, s));
+    KMC_CUDA_TRY(cudaMemcpyAsync(out, sum, sizeof(double), cudaMemcpyDeviceToHost, s));
+    KMC_CUDA_TRY(cudaStreamSynchronize(s));
     return KMC_OK;
 }
 
@@ -465,6 +498,8 @@ struct Active {
     int64_t req = -1;
     int64_t inst = -1;                 // plain: batch instance
     std::unique_ptr<FitBase> fit;      // mixed: tensor-core fit session
+    cudaEvent_t ev = nullptr;          // mixed: a transform's distances are written
+    cudaStream_t st = nullptr;         // the request's stream
     int stream = 0;
     int64_t bytes = 0;
     std::unique_ptr<ReqMem> mem;
@@ -480,17 +515,18 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
                   "unknown form %d", form);
     for (int64_t r = 0; r < n_req; ++r) {
         const kmc_serve_request_t &q = rq[r];
-        KMC_CHECK_ARG(q.kind == 0 || q.kind == 1, "request %lld: kind must be 0 or 1",
+        KMC_CHECK_ARG(q.kind >= 0 && q.kind <= 2, "request %lld: kind must be 0, 1 or 2",
                       (long long)r);
         KMC_CHECK_ARG(q.n_samples >= 1 && q.n_features >= 1 && q.n_clusters >= 1 &&
-                          (q.kind == 1 || q.n_clusters <= q.n_samples) && q.n_centers >= 1,
+                          (q.kind != 0 || q.n_clusters <= q.n_samples) && q.n_centers >= 1,
                       "request %lld: invalid sizes", (long long)r);
         KMC_CHECK_ARG(r == 0 || q.arrival_s >= rq[r - 1].arrival_s,
                       "requests must be sorted by arrival time");
         KMC_CHECK_ARG(q.kind == 0 || (q.model >= 0 && q.model < r && rq[q.model].kind == 0 &&
                                       rq[q.model].n_features == q.n_features &&
                                       rq[q.model].n_clusters == q.n_clusters),
-                      "request %lld: a prediction must name an earlier fit of the same d, k",
+                      "request %lld: a prediction or transform must name an earlier fit of "
+                      "the same d, k",
                       (long long)r);
         out[r] = kmc_serve_result_t{-1.0, -1.0, 0, 0.0, KMC_OK, 0};
     }
@@ -529,6 +565,12 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
     auto finish = [&](Active &a, int64_t n_iter, double inertia, int status) -> int {
         const kmc_serve_request_t &q = rq[a.req];
         kmc_serve_result_t &o = out[a.req];
+        if (status == KMC_OK && q.kind == 2)
+            KMC_TRY(dist_checksum(*a.mem, q.n_samples, q.n_clusters, a.st, &inertia));
+        if (a.ev) {
+            cudaEventDestroy(a.ev);
+            a.ev = nullptr;
+        }
         if (status == KMC_OK && q.kind == 0) {
             std::vector<float> &m = models[(size_t)a.req];
             m.resize((size_t)(q.n_features * q.n_clusters));
@@ -555,7 +597,8 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
         const int64_t n = q.n_samples, d = q.n_features, k = q.n_clusters;
         cudaStream_t st = plain ? s : pool[(size_t)(rr++ % kStreams)];
         a->stream = plain ? 0 : (int)((rr - 1) % kStreams);
-        KMC_TRY(alloc_request(*a->mem, n, d, k, st));
+        a->st = st;
+        KMC_TRY(alloc_request(*a->mem, n, d, k, q.kind, st));
         ReqMem &m = *a->mem;
         KMC_TRY(launch_blobs(m.X, n, d, q.n_centers, -10.f, 10.f, q.std_lo, q.std_hi, q.seed, st));
         KMC_TRY(launch_fill<float>(m.w, 1.f, n, st));
@@ -579,8 +622,17 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
             if (q.kind == 0)
                 KMC_TRY(eng.add(B_FIT, m.X, m.w, m.C, m.labels, n, d, k, q.tol, q.max_iter,
                                 &a->inst));
-            else
+            else if (q.kind == 1)
                 KMC_TRY(eng.add(B_ASSIGN, m.X, nullptr, m.C, m.labels, n, d, k, 0.0, 0, &a->inst));
+            else
+                KMC_TRY(eng.add(B_TRANSFORM, m.X, nullptr, m.C, nullptr, n, d, k, 0.0, 0,
+                                &a->inst, m.dist));
+        } else if (q.kind == 2) {
+            // exact float32 distances (no tensor-core form of the distance
+            // matrix), on the request's stream
+            KMC_TRY(launch_distances<float>(m.X, m.C, m.dist, n, d, k, st));
+            KMC_CUDA_TRY(cudaEventCreateWithFlags(&a->ev, cudaEventDisableTiming));
+            KMC_CUDA_TRY(cudaEventRecord(a->ev, st));
         } else {
             FitParams<float, int32_t> p;
             p.X = m.X;
@@ -608,7 +660,7 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
         // queue) until their model has been fitted
         for (auto it = pending.begin(); it != pending.end();) {
             const kmc_serve_request_t &q = rq[*it];
-            if (q.kind == 1 && !model_ready[(size_t)q.model]) {
+            if (q.kind != 0 && !model_ready[(size_t)q.model]) {
                 ++it;
                 continue;
             }
@@ -659,6 +711,7 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
             // one iteration of every running session, overlapped across streams
             std::vector<int> was_done(active.size(), 0);
             for (size_t t = 0; t < active.size(); ++t) {
+                if (!active[t]->fit) continue;  // a transform in flight
                 LoopState st{};
                 KMC_TRY(active[t]->fit->read_state(st));
                 was_done[t] = st.done;
@@ -666,6 +719,17 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
             }
             for (size_t t = 0; t < active.size();) {
                 Active &a = *active[t];
+                if (!a.fit) {
+                    const cudaError_t q = cudaEventQuery(a.ev);
+                    if (q == cudaErrorNotReady) {
+                        ++t;
+                        continue;
+                    }
+                    KMC_CUDA_TRY(q);
+                    KMC_TRY(finish(a, 0, 0.0, KMC_OK));
+                    active.erase(active.begin() + (int64_t)t);
+                    continue;
+                }
                 LoopState st{};
                 KMC_TRY(a.fit->read_state(st));
                 if (st.done) {
@@ -722,6 +786,15 @@ int kmc_batch_add_predict_f32(kmc_batch_t batch, const float *X_t, const float *
     KMC_CHECK_ARG(batch != nullptr && instance_out != nullptr, "null argument");
     return batch->eng.add(B_ASSIGN, X_t, nullptr, const_cast<float *>(centroids_t), labels,
                           n_samples, n_features, n_clusters, 0.0, 0, instance_out);
+}
+
+int kmc_batch_add_transform_f32(kmc_batch_t batch, const float *X_t, const float *centroids_t,
+                                float *distances, int64_t n_samples, int64_t n_features,
+                                int64_t n_clusters, int64_t *instance_out) {
+    KMC_CHECK_ARG(batch != nullptr && instance_out != nullptr, "null argument");
+    KMC_CHECK_ARG(distances != nullptr || n_samples == 0, "null distances");
+    return batch->eng.add(B_TRANSFORM, X_t, nullptr, const_cast<float *>(centroids_t), nullptr,
+                          n_samples, n_features, n_clusters, 0.0, 0, instance_out, distances);
 }
 
 int kmc_batch_step(kmc_batch_t batch, int64_t *n_active_out) {
@@ -798,7 +871,7 @@ int kmc_seeded_rows(int64_t n_samples, int64_t n_clusters, uint64_t seed, int32_
 int kmc_serve_bytes_needed(int32_t kind, int64_t n_samples, int64_t n_features,
                            int64_t n_clusters, int form, int64_t *bytes_out) {
     KMC_CHECK_ARG(bytes_out != nullptr, "null output");
-    KMC_CHECK_ARG(kind == 0 || kind == 1, "kind must be 0 (fit) or 1 (predict)");
+    KMC_CHECK_ARG(kind >= 0 && kind <= 2, "kind must be 0 (fit), 1 (predict) or 2 (transform)");
     KMC_CHECK_ARG(n_samples >= 0 && n_features >= 1 && n_clusters >= 1, "invalid sizes");
     *bytes_out = request_bytes(kind, n_samples, n_features, n_clusters, form);
     return KMC_OK;

@@ -48,7 +48,8 @@ def _reqs(rows):
      "sorted by arrival"),
     ([(0.0, 1, 4, 100, 8, 2, 1, 0.0, 0, 0, 1.0, 1.0)], "earlier fit"),
     ([(0.0, 0, 4, 10, 80, 2, 1, 0.0, 10, -1, 1.0, 1.0)], "invalid sizes"),
-    ([(0.0, 2, 4, 100, 8, 2, 1, 0.0, 10, -1, 1.0, 1.0)], "kind must be"),
+    ([(0.0, 3, 4, 100, 8, 2, 1, 0.0, 10, -1, 1.0, 1.0)], "kind must be"),
+    ([(0.0, 2, 4, 100, 8, 2, 1, 0.0, 0, 0, 1.0, 1.0)], "earlier fit"),   # transform without a model
 ])
 def test_serve_run_rejects_bad_request_streams(rows, msg):
     L = capi.lib()

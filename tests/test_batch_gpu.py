@@ -275,3 +275,86 @@ def test_serving_admission_respects_the_memory_budget():
     for a, b in zip(order, order[1:]):
         assert res[b].admit_s >= res[a].finish_s - 1e-6
     assert all(r.status == 0 for r in res)
+
+
+def _distances_single(X, C):
+    import torch
+
+    capi, L = _lib()
+    d, n = X.shape
+    k = C.shape[1]
+    Xg = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+    Cg = torch.from_numpy(np.ascontiguousarray(C)).cuda()
+    out = torch.empty((k, n), dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream()
+    capi.check(L.kmc_compute_centroid_to_sample_distances_f32(Xg.data_ptr(), Cg.data_ptr(),
+                                                              out.data_ptr(), n, d, k, 256, 128,
+                                                              s.cuda_stream))
+    s.synchronize()
+    return out.cpu().numpy()
+
+
+def test_batched_transforms_equal_single_distance_calls(oracle):
+    """Transform instances run through the persistent tiles beside fits and
+    predictions; their distances are bit-equal to the single-call kernel's
+    and match the oracle's."""
+    import torch
+
+    rng = np.random.default_rng(21)
+    b = Batch()
+    try:
+        outs = []
+        fitX, fitC, tol, mi = _case_data(CASES[0])
+        b.add_fit(fitX, fitC, tol, mi)
+        for n, d, k in [(1000, 5, 7), (20001, 64, 300), (257, 129, 33), (4096, 16, 1024)]:
+            X = rng.standard_normal((d, n)).astype(np.float32)
+            C = rng.standard_normal((d, k)).astype(np.float32)
+            Xg = torch.from_numpy(X).cuda()
+            Cg = torch.from_numpy(C).cuda()
+            D = torch.full((k, n), -1.0, dtype=torch.float32, device="cuda")
+            inst = ctypes.c_int64()
+            b.capi.check(b.L.kmc_batch_add_transform_f32(b.h, Xg.data_ptr(), Cg.data_ptr(),
+                                                         D.data_ptr(), n, d, k, ctypes.byref(inst)))
+            b.keep[inst.value] = (Xg, None, Cg, D)
+            outs.append((inst.value, X, C, D))
+            if n == 257:
+                b.add_predict(X, C)
+        b.run()
+        for inst, X, C, D in outs:
+            fin, it, _, _, _ = b.result(inst)
+            assert fin and it == 0
+            got = D.cpu().numpy()
+            np.testing.assert_array_equal(got, _distances_single(X, C))
+            np.testing.assert_array_equal(got, oracle.distances(X, C))
+    finally:
+        b.close()
+
+
+@pytest.mark.parametrize("form", [0, 2])
+def test_serving_transforms_match_transforms_served_alone(form):
+    """Transform requests (kind 2) in a mix of fits and predictions give the
+    float64 total of their distance matrix that the same request gives when
+    served right after its model alone."""
+    spec = SPEC + [(0.032, 2, 7000, 16, 24, 8, 0.0, 0, 0),
+                   (0.033, 2, 3000, 64, 300, 9, 0.0, 0, 2),
+                   (0.034, 1, 2000, 16, 8, 10, 0.0, 0, 4)]
+    mixed, _ = _serve(spec, form)
+    assert all(o.status == 0 for o in mixed)
+    for r, s in enumerate(spec):
+        if s[1] != 2:
+            continue
+        assert mixed[r].n_iter == 0 and mixed[r].inertia > 0
+        fit = (0.0,) + spec[s[8]][1:]
+        alone, _ = _serve([fit, (0.0,) + s[1:8] + (0,)], form)
+        assert alone[1].status == 0
+        assert alone[1].inertia == pytest.approx(mixed[r].inertia, rel=1e-5)
+
+
+def test_serving_sizes_transform_requests():
+    from kmeans_dpcpp_gb300 import capi
+
+    _, L = _lib()
+    a, b = ctypes.c_int64(), ctypes.c_int64()
+    capi.check(L.kmc_serve_bytes_needed(1, 100000, 32, 256, 0, ctypes.byref(a)))
+    capi.check(L.kmc_serve_bytes_needed(2, 100000, 32, 256, 0, ctypes.byref(b)))
+    assert b.value >= a.value + 4 * 100000 * 256
