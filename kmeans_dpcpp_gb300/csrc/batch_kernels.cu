@@ -284,7 +284,9 @@ __global__ void __launch_bounds__(kThreadsB, 2)
                     const int64_t f = e / BM;
                     const int64_t i = i0 + s;
                     if (i < n) {
-                        const float v = __fmul_rn(X[f * n + i], ws[s]);
+                        // up to kBK features the samples are still in chunk buffer 0
+                        const float x = (nchunks == 1) ? Xs[f * BM + s] : X[f * n + i];
+                        const float v = __fmul_rn(x, ws[s]);
                         atomicAdd(&tsums[f * k + labs[s]], (double)v);
                     }
                 }
