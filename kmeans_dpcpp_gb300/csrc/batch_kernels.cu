@@ -40,6 +40,7 @@ constexpr int kThreadsB = 256;
 constexpr int kBK = 16;
 constexpr int kTM = 8;
 constexpr size_t kPrivBytes = 72 * 1024;  // with the tiles: two CTAs per SM
+constexpr int kSumCopies = 48;            // global copies of small instances' sums
 
 // Deterministic block-wide float64 sum (same shape as the single-fit loop
 // control: warp shuffles, then warp 0 over the warp totals).
@@ -71,7 +72,7 @@ __global__ void batch_prep_kernel(BInst *tab, const int *idx, int count, int *co
         in.hn[j] = acc / 2.f;
     }
     if (in.mode == B_FIT) {
-        const int64_t total = (int64_t)d * k + k;
+        const int64_t total = ((int64_t)d * k + k) * in.copies;
         for (int64_t e = threadIdx.x; e < total; e += blockDim.x) in.sums[e] = 0.0;
         if (threadIdx.x == 0) in.empty_list[k] = 0;
     }
@@ -134,8 +135,8 @@ __global__ void __launch_bounds__(kThreadsB, 2)
         const int d = in.d, k = in.k;
         const bool fit = in.mode == B_FIT;
         const int64_t dk = (int64_t)d * k;
-        const bool priv = fit && (size_t)(dk + k) * sizeof(double) <= kPrivBytes;
-        double *tsums = priv ? psums : in.sums;
+        const bool priv = fit && in.copies == 1 && (size_t)(dk + k) * sizeof(double) <= kPrivBytes;
+        double *tsums = priv ? psums : in.sums + (int64_t)(blockIdx.x % (unsigned)in.copies) * (dk + k);
         double *tsizes = tsums + dk;
         if (priv) {
             for (int64_t e = tid; e < dk + k; e += kThreadsB) psums[e] = 0.0;
@@ -313,7 +314,8 @@ __global__ void batch_reduce_kernel(BInst *tab, const int *idx, int count, int *
     const int d = in.d, k = in.k;
     const int64_t dk = (int64_t)d * k;
     for (int64_t e = threadIdx.x; e < dk + k; e += blockDim.x) {
-        const double s = 0.0 + in.sums[e];
+        double s = 0.0;
+        for (int c = 0; c < in.copies; ++c) s += in.sums[(int64_t)c * (dk + k) + e];
         if (e < dk)
             in.Cn[e] = (float)s;
         else
@@ -519,6 +521,10 @@ void tune_store(int64_t d, int64_t k, int v) {
 
 int batch_variant_width(int v) { return v == 0 ? 32 : (v == 1 ? 64 : 128); }
 
+int batch_sum_copies(int64_t d, int64_t k) {
+    return ((d + 1) * k * (int64_t)sizeof(double) <= (int64_t)kPrivBytes) ? kSumCopies : 1;
+}
+
 size_t batch_assign_smem(int v) {
     const size_t b = v == 0 ? BTile<2>::base_bytes
                             : (v == 1 ? BTile<4>::base_bytes : BTile<8>::base_bytes);
@@ -638,6 +644,7 @@ int tune_variant(int64_t d, int64_t k_in, cudaStream_t s, int *variant) {
     h.C = C;
     h.hn = reinterpret_cast<float *>(b + off_hn);
     h.sums = reinterpret_cast<double *>(b + off_sum);
+    h.copies = 1;
     h.labels = reinterpret_cast<int32_t *>(b + off_lab);
     h.n = n;
     h.d = (int)d;

@@ -32,6 +32,7 @@ struct BInst {
     int d, k;
     int mode;              // B_FIT or B_ASSIGN
     int variant;           // centroid-window width: 0 -> 32, 1 -> 64, 2 -> 128
+    int copies;            // private copies of sums (CTA b adds into copy b % copies)
     LoopState st;          // done / n_iter / max_iter / tol / last_shift
 };
 
@@ -46,6 +47,9 @@ constexpr int kBatchVariants = 3;
 constexpr int kBatchTileM = 128;
 
 int batch_variant_width(int v);
+// Private global copies of an instance's float64 sums: small sums get several
+// (their few addresses would serialise the reductions of many CTAs).
+int batch_sum_copies(int64_t d, int64_t k);
 // Dynamic shared memory of one assign CTA of variant v.
 size_t batch_assign_smem(int v);
 

@@ -44,7 +44,8 @@ struct SlotMem {
 size_t slot_bytes(int mode, int64_t n, int64_t d, int64_t k) {
     size_t b = align256(sizeof(float) * d * k) + 2 * align256(sizeof(float) * k);
     if (mode == B_FIT) {
-        b += align256(sizeof(double) * (d * k + k)) + align256(sizeof(int32_t) * (k + 1)) +
+        b += align256(sizeof(double) * (d * k + k) * batch_sum_copies(d, k)) +
+             align256(sizeof(int32_t) * (k + 1)) +
              align256(sizeof(float) * n) + align256(sizeof(int32_t) * (n + 2)) +
              align256(sizeof(float)) + align256(threshold_scratch_bytes()) +
              align256(select_scratch_bytes(k)) + align256(sizeof(double) * sum_partials_size()) +
@@ -66,7 +67,7 @@ int alloc_slot(SlotMem &m, int mode, int64_t n, int64_t d, int64_t k, cudaStream
     m.hn = reinterpret_cast<float *>(take(sizeof(float) * k));
     m.sizes = reinterpret_cast<float *>(take(sizeof(float) * k));
     if (mode == B_FIT) {
-        m.sums = reinterpret_cast<double *>(take(sizeof(double) * (d * k + k)));
+        m.sums = reinterpret_cast<double *>(take(sizeof(double) * (d * k + k) * batch_sum_copies(d, k)));
         m.empty_list = reinterpret_cast<int32_t *>(take(sizeof(int32_t) * (k + 1)));
         m.sq_dist = reinterpret_cast<float *>(take(sizeof(float) * n));
         m.selected = reinterpret_cast<int32_t *>(take(sizeof(int32_t) * (n + 2)));
@@ -226,6 +227,7 @@ struct BatchEngine {
         h.hn = m->hn;
         h.sizes = m->sizes;
         h.sums = m->sums;
+        h.copies = mode == B_FIT ? batch_sum_copies(d, k) : 1;
         h.labels = labels;
         h.dist = dist;
         h.empty_list = m->empty_list;
