@@ -143,8 +143,40 @@ __global__ void __launch_bounds__(kThreadsB, 2)
             __syncthreads();
         }
         const int nchunks = (d + kBK - 1) / kBK;
+        const int64_t tile_end = item.tile0 + item.ntiles;
+        // Feature chunk ch of samples li0.. and centroids lc0.. into registers;
+        // chunk 0 of the item's next (tile, centroid window) step is loaded
+        // while the current step's last chunk is multiplied (the widest
+        // window has no registers to spare for it: it loads at the step).
+        constexpr bool kAhead = TN <= 4;
+        float xr[XR], cr[CR];
+        auto load_regs = [&](int64_t li0, int lc0, int ch) {
+            const int f0 = ch * kBK;
+#pragma unroll
+            for (int r = 0; r < XR; ++r) {
+                const int e = tid + r * kThreadsB;
+                const int kk = e / BM, s = e % BM;
+                const int f = f0 + kk;
+                const int64_t i = li0 + s;
+                xr[r] = (f < d && i < n) ? X[(int64_t)f * n + i] : 0.f;
+            }
+#pragma unroll
+            for (int r = 0; r < CR; ++r) {
+                const int e = tid + r * kThreadsB;
+                const int kk = e / BN, c = e % BN;
+                const int f = f0 + kk, j = lc0 + c;
+                cr[r] = (f < d && j < k) ? C[(int64_t)f * k + j] : 0.f;
+            }
+        };
+        auto store_smem = [&](int buf) {
+#pragma unroll
+            for (int r = 0; r < XR; ++r) Xs[buf * kBK * BM + tid + r * kThreadsB] = xr[r];
+#pragma unroll
+            for (int r = 0; r < CR; ++r) Cs[buf * kBK * BN + tid + r * kThreadsB] = cr[r];
+        };
+        if (kAhead) load_regs(item.tile0 * BM, 0, 0);
 
-        for (int64_t tile = item.tile0; tile < item.tile0 + item.ntiles; ++tile) {
+        for (int64_t tile = item.tile0; tile < tile_end; ++tile) {
             const int64_t i0 = tile * BM;
             float best[kTM];
             int bidx[kTM];
@@ -162,37 +194,17 @@ __global__ void __launch_bounds__(kThreadsB, 2)
                 for (int c = tid; c < BN; c += kThreadsB)
                     hs[c] = (c0 + c < k) ? hn[c0 + c] : pos_inf<float>();
 
-                float xr[XR], cr[CR];
-                auto load_regs = [&](int ch) {
-                    const int f0 = ch * kBK;
-#pragma unroll
-                    for (int r = 0; r < XR; ++r) {
-                        const int e = tid + r * kThreadsB;
-                        const int kk = e / BM, s = e % BM;
-                        const int f = f0 + kk;
-                        const int64_t i = i0 + s;
-                        xr[r] = (f < d && i < n) ? X[(int64_t)f * n + i] : 0.f;
-                    }
-#pragma unroll
-                    for (int r = 0; r < CR; ++r) {
-                        const int e = tid + r * kThreadsB;
-                        const int kk = e / BN, c = e % BN;
-                        const int f = f0 + kk, j = c0 + c;
-                        cr[r] = (f < d && j < k) ? C[(int64_t)f * k + j] : 0.f;
-                    }
-                };
-                auto store_smem = [&](int buf) {
-#pragma unroll
-                    for (int r = 0; r < XR; ++r) Xs[buf * kBK * BM + tid + r * kThreadsB] = xr[r];
-#pragma unroll
-                    for (int r = 0; r < CR; ++r) Cs[buf * kBK * BN + tid + r * kThreadsB] = cr[r];
-                };
-                load_regs(0);
-                store_smem(0);
+                if (!kAhead) load_regs(i0, c0, 0);
+                store_smem(0);  // chunk 0 (loaded during the previous step when kAhead)
                 __syncthreads();
                 for (int ch = 0; ch < nchunks; ++ch) {
                     const int buf = ch & 1;
-                    if (ch + 1 < nchunks) load_regs(ch + 1);
+                    if (ch + 1 < nchunks)
+                        load_regs(i0, c0, ch + 1);
+                    else if (kAhead && c0 + BN < k)
+                        load_regs(i0, c0 + BN, 0);
+                    else if (kAhead && tile + 1 < tile_end)
+                        load_regs(i0 + BM, 0, 0);
                     const float *xb = Xs + buf * kBK * BM;
                     const float *cb = Cs + buf * kBK * BN;
 #pragma unroll
