@@ -262,28 +262,13 @@ __global__ void __launch_bounds__(kThreadsB, 2)
             }
             if (DIST) continue;
             // (value, index) minimum over the 16 threads sharing these samples
-#pragma unroll
-            for (int m = 0; m < kTM; ++m) {
-                float v = best[m];
-                int j = bidx[m];
-#pragma unroll
-                for (int off = 8; off > 0; off >>= 1) {
-                    const float ov = __shfl_xor_sync(0xffffffffu, v, off);
-                    const int oj = __shfl_xor_sync(0xffffffffu, j, off);
-                    if (ov < v || (ov == v && oj < j)) {
-                        v = ov;
-                        j = oj;
-                    }
-                }
-                bidx[m] = j;
-            }
-#pragma unroll
-            for (int m = 0; m < kTM; ++m) {
-                if (tx == m) {
+            {
+                const int m = rowmin16<float, kTM>(best, bidx, tx);
+                if ((tx & (16 / kTM - 1)) == 0) {
                     const int s = (m < HM) ? ty * HM + m : BM / 2 + ty * HM + (m - HM);
                     const int64_t i = i0 + s;
-                    if (i < n) labels[i] = bidx[m];
-                    labs[s] = bidx[m];
+                    if (i < n) labels[i] = bidx[0];
+                    labs[s] = bidx[0];
                 }
             }
             if (fit) {

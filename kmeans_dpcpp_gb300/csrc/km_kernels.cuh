@@ -22,6 +22,54 @@ struct LoopState {
     unsigned int pad;
 };
 
+// Lexicographic (value, index) minimum of each of the TM sample rows a thread
+// holds over the 16 threads (lanes differing in bits 0-3, tx = lane & 15) that
+// hold the same rows -- the first minimum of a sequential strict-< scan over
+// ascending index.  Recursive halving: at offset o the lower thread of a pair
+// keeps the first half of its remaining rows and the upper thread the second,
+// each combining its own candidate with the partner's for the rows it keeps;
+// once one row is left, partners combine it.  Returns the row (0..TM-1) whose
+// result this thread ends with in v[0], j[0]; 16 / TM threads end with each
+// row, the lowest of them has (tx & (16 / TM - 1)) == 0.  Values are never NaN
+// (they come from strict-< updates of +inf).
+template <typename T, int TM>
+__device__ __forceinline__ int rowmin16(T (&v)[TM], int (&j)[TM], int tx) {
+    int base = 0;
+    int R = TM;
+#pragma unroll
+    for (int off = 8; off > 0; off >>= 1) {
+        if (R >= 2) {
+            const int H = R / 2;
+            const bool upper = (tx & off) != 0;
+#pragma unroll
+            for (int r = 0; r < H; ++r) {
+                const T sv = upper ? v[r] : v[r + H];
+                const int sj = upper ? j[r] : j[r + H];
+                T kv = upper ? v[r + H] : v[r];
+                int kj = upper ? j[r + H] : j[r];
+                const T ov = __shfl_xor_sync(0xffffffffu, sv, off);
+                const int oj = __shfl_xor_sync(0xffffffffu, sj, off);
+                if (ov < kv || (ov == kv && oj < kj)) {
+                    kv = ov;
+                    kj = oj;
+                }
+                v[r] = kv;
+                j[r] = kj;
+            }
+            if (upper) base += H;
+            R = H;
+        } else {
+            const T ov = __shfl_xor_sync(0xffffffffu, v[0], off);
+            const int oj = __shfl_xor_sync(0xffffffffu, j[0], off);
+            if (ov < v[0] || (ov == v[0] && oj < j[0])) {
+                v[0] = ov;
+                j[0] = oj;
+            }
+        }
+    }
+    return base;
+}
+
 // ---- kernels_util.cu ----
 template <typename T>
 int launch_broadcast_divide(T *X, const T *y, int64_t rows, int64_t cols, cudaStream_t s);
