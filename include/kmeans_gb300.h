@@ -5,7 +5,7 @@
  * (python_api/_kmeans_lloyd.cpp).  Each entry point replaces one templated
  * SYCL host function that the reference's pybind11 wrappers dispatch to; the
  * comment above each group cites the wrapper (python_api/_kmeans_lloyd.cpp)
- * and the kernel header (src/*.hpp) it replaces.
+ * and the kernel header (a src/ .hpp file) it replaces.
  *
  * Conventions
  *  - All array arguments are device pointers to C-contiguous arrays, in the
