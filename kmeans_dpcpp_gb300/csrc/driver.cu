@@ -17,6 +17,7 @@
 // one iteration body works for every iteration (and can be captured once
 // into a CUDA graph).  The convergence total and the final inertia are summed
 // in float64.
+#include <algorithm>
 #include <cstdarg>
 #include <memory>
 #include <vector>
@@ -34,7 +35,15 @@ int PlainFit<T, I>::init(const FitParams<T, I> &p) {
     // Small sums get one float64 copy per CTA of the fused step (two CTAs
     // per SM), filled with fire-and-forget global reductions; shared-memory
     // float64 atomics would be compare-and-swap loops on the critical path.
-    P = ((d + 1) * k <= 8192) ? 2 * (int64_t)num_sms() : 1;
+    // float64 samples get a copy per CTA up to 256 MiB of copies: each CTA
+    // then sums its samples in a fixed order (bit-reproducible centroids).
+    if (sizeof(T) == 8) {
+        const int64_t per_copy = 8 * (d + 1) * std::max<int64_t>(k, 1);
+        P = std::max<int64_t>(1, std::min<int64_t>(2 * (int64_t)num_sms(),
+                                                   (int64_t(256) << 20) / per_copy));
+    } else {
+        P = ((d + 1) * k <= 8192) ? 2 * (int64_t)num_sms() : 1;
+    }
     size_t off = 0;
     auto take = [&](size_t bytes) {
         size_t o = off;

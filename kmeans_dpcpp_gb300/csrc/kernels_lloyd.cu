@@ -18,10 +18,19 @@
 // argmin of each sample is reduced across the 16 threads that share it with
 // warp shuffles.  Centroid sums are privatised per CTA in shared memory when
 // (d + 1) * k fits, and flushed once per CTA with atomics; otherwise they go
-// straight to the global private copy with atomics.  float64 sums with one
-// global copy per CTA always take the global route: float64 reductions to
-// global memory are native (fire-and-forget), in shared memory they are
-// compare-and-swap loops.
+// straight to the global private copy with atomics.  float64 sums of float
+// samples with one global copy per CTA take the global route: float64
+// reductions to global memory are native (fire-and-forget), in shared memory
+// they are compare-and-swap loops.
+//
+// float64 samples are summed in a deterministic order whenever every CTA has a
+// copy of its own: thread t of a CTA owns clusters j = t (mod 256) and adds
+// each tile's samples in ascending order with plain read-modify-writes (in
+// shared memory when the sums fit there), and the copies are reduced in copy
+// order.  A fit whose labels stop changing then reproduces its centroids bit
+// for bit, so a zero tolerance stops it on the same iteration as a sequential
+// implementation (atomics in arbitrary order leave last-bit noise in every
+// centroid shift).
 #include "km_kernels.cuh"
 
 namespace kmc {
@@ -62,6 +71,7 @@ struct TileArgs {
     T *dist;
     int64_t n, d, k, P;
     int priv;
+    int owned;  // every CTA has a copy of its own (float64 samples: ordered sums)
     const LoopState *guard;
 };
 
@@ -283,7 +293,24 @@ __global__ void __launch_bounds__(kThreads, 2) tile_kernel(TileArgs<T, I, A> a) 
             __syncthreads();
             A *tsums = a.priv ? psums : gsums;
             A *tsizes = a.priv ? psizes : gsizes;
-            for (int64_t e = tid; e < (int64_t)BM * d; e += kThreads) {
+            bool ordered = false;
+            if constexpr (sizeof(T) == 8) {
+                if (a.owned) {
+                    ordered = true;
+                    static_assert((kThreads & (kThreads - 1)) == 0, "power-of-two CTA");
+                    for (int s = 0; s < BM; ++s) {
+                        const int64_t j = labs[s];
+                        if (i0 + s >= n || (int)(j & (kThreads - 1)) != tid) continue;
+                        const T wv = ws[s];
+                        for (int64_t f = 0; f < d; ++f) {
+                            const T xv = (nchunks == 1) ? Xs[f * BM + s] : a.X[f * n + i0 + s];
+                            tsums[f * k + j] += (A)mul_rn(xv, wv);
+                        }
+                        tsizes[j] += (A)wv;
+                    }
+                }
+            }
+            for (int64_t e = tid; !ordered && e < (int64_t)BM * d; e += kThreads) {
                 int s = (int)(e % BM);
                 int64_t f = e / BM;
                 int64_t i = i0 + s;
@@ -295,7 +322,7 @@ __global__ void __launch_bounds__(kThreads, 2) tile_kernel(TileArgs<T, I, A> a) 
                     atomicAdd(&tsums[f * k + labs[s]], (A)val);
                 }
             }
-            for (int s = tid; s < BM; s += kThreads) {
+            for (int s = tid; !ordered && s < BM; s += kThreads) {
                 int64_t i = i0 + s;
                 if (i < n) atomicAdd(&tsizes[labs[s]], (A)ws[s]);
             }
@@ -317,7 +344,7 @@ __global__ void __launch_bounds__(kThreads, 2) tile_kernel(TileArgs<T, I, A> a) 
 }
 
 template <typename T, typename I, int MODE, typename A = T>
-int launch_tile(const TileArgs<T, I, A> &args, cudaStream_t s) {
+int launch_tile(TileArgs<T, I, A> args, cudaStream_t s) {
     if (args.n == 0) return KMC_OK;
     size_t smem = TileSmem<T>::base_bytes;
     if (MODE == MODE_FUSED && args.priv) smem += sizeof(A) * (size_t)(args.d * args.k + args.k);
@@ -334,6 +361,7 @@ int launch_tile(const TileArgs<T, I, A> &args, cudaStream_t s) {
     if (MODE == MODE_DIST) grid = tiles;  // output-bound: one tile per CTA
     if (grid > tiles) grid = tiles;
     if (grid > (1LL << 30)) grid = 1LL << 30;
+    args.owned = (MODE == MODE_FUSED && sizeof(T) == 8 && args.P >= grid) ? 1 : 0;
     kern<<<(unsigned)grid, kThreads, smem, s>>>(args);
     return check_launch("tile_kernel");
 }
@@ -343,7 +371,8 @@ int launch_tile(const TileArgs<T, I, A> &args, cudaStream_t s) {
 template <typename T, typename I>
 int launch_assignment(const T *X, const T *C, const T *hn, I *labels, int64_t n, int64_t d,
                       int64_t k, cudaStream_t s, const LoopState *guard) {
-    TileArgs<T, I> a{X, nullptr, C, hn, labels, nullptr, nullptr, nullptr, n, d, k, 1, 0, guard};
+    TileArgs<T, I> a{X, nullptr, C, hn, labels, nullptr, nullptr, nullptr, n, d, k, 1, 0, 0,
+                     guard};
     return launch_tile<T, I, MODE_ASSIGN>(a, s);
 }
 
@@ -351,12 +380,13 @@ template <typename T, typename I, typename A>
 int launch_fused_step(const T *X, const T *w, const T *C, const T *hn, I *labels, A *sums_cp,
                       A *sizes_cp, int64_t n, int64_t d, int64_t k, int64_t P, cudaStream_t s,
                       const LoopState *guard) {
-    // float64 sums with one copy per CTA go straight to global memory
-    // (native reductions); otherwise small sums are privatised in shared memory
-    int priv = (sizeof(A) * (size_t)(d * k + k) <= kPrivMaxBytes && !(sizeof(A) == 8 && P > 1))
-                   ? 1
-                   : 0;
-    TileArgs<T, I, A> a{X, w, C, hn, labels, sums_cp, sizes_cp, nullptr, n, d, k, P, priv, guard};
+    // float64 sums of float samples with one copy per CTA go straight to
+    // global memory (native reductions); otherwise small sums are privatised
+    // in shared memory (float64 samples: ordered plain updates, no atomics)
+    const bool fits = sizeof(A) * (size_t)(d * k + k) <= kPrivMaxBytes;
+    int priv = (fits && (sizeof(T) == 8 || !(sizeof(A) == 8 && P > 1))) ? 1 : 0;
+    TileArgs<T, I, A> a{X, w, C, hn, labels, sums_cp, sizes_cp, nullptr, n, d, k, P, priv, 0,
+                        guard};
     return launch_tile<T, I, MODE_FUSED, A>(a, s);
 }
 
@@ -364,7 +394,7 @@ template <typename T>
 int launch_distances(const T *X, const T *C, T *out, int64_t n, int64_t d, int64_t k,
                      cudaStream_t s) {
     TileArgs<T, int32_t> a{X, nullptr, C, nullptr, nullptr, nullptr, nullptr, out,
-                           n, d, k, 1, 0, nullptr};
+                           n, d, k, 1, 0, 0, nullptr};
     return launch_tile<T, int32_t, MODE_DIST>(a, s);
 }
 

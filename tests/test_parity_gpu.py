@@ -187,6 +187,9 @@ DRIVER_CASES = {
     "c2_small_forced_empty": (200_000, 14, 127, 127, (-10, 10), 1.5, 1, 0.0, 12, True),
     "d64_k256": (60_000, 64, 256, 256, (-5, 5), 1.0, 2, 0.0, 6, False),
     "more_clusters_than_blobs": (30_000, 5, 4, 40, (-10, 10), 1.0, 3, 1e-6, 30, False),
+    # zero tolerance, converging long before max_iter: the stop needs a centroid
+    # shift of exactly zero once the labels settle
+    "converges_tol0": (300_000, 3, 6, 6, (-10, 10), 0.7, 5, 0.0, 200, False),
 }
 
 
@@ -204,6 +207,19 @@ def test_driver_parity(kdp, oracle, case, dt):
     assert inr_g == pytest.approx(inr_o, rel=RTOL_C[dt])
     if far:
         assert rel_o >= 1  # the forced empty cluster was relocated
+
+
+def test_driver_float64_reproducible(kdp):
+    """float64 fits sum each CTA's samples in a fixed order: two runs of the same fit give
+    the same bits, and a zero tolerance stops once the labels settle."""
+    X, _, _ = bench.make_blobs(400_000, 5, 20, (-10, 10), 1.0, 11, dtype=np.float64)
+    C0 = bench.random_row_init(X, 20, 11)
+    r1 = _run_driver(kdp, X, C0, 0.0, 300)
+    r2 = _run_driver(kdp, X, C0, 0.0, 300)
+    assert r1[0] == r2[0] < 300
+    np.testing.assert_array_equal(r1[1], r2[1])
+    np.testing.assert_array_equal(r1[2], r2[2])
+    assert r1[3] == r2[3]
 
 
 @pytest.mark.parametrize("n,d,k", [(5, 3, 8), (1, 2, 3), (40, 1, 1), (3, 4, 3)])
