@@ -96,14 +96,22 @@ def _near_tie_mask(X, C, rel=1e-5):
 
 # Up to 32 features the cluster sums are reduced in float64, so whole
 # trajectories follow the oracle's (iteration count included).
+# The forced-empty case relocates a cluster in its first iteration: the samples moved
+# are chosen by the squared distances the assignment pass writes.
 @pytest.mark.parametrize("case", [("c1_50k_d14_k16", 50_000, 14, 16, 16, (-10, 10), 1.0, 0, 1e-4, 100),
-                                  ("d32_k200", 40_000, 32, 100, 200, (-5, 5), 1.0, 3, 0.0, 10)])
+                                  ("d32_k200", 40_000, 32, 100, 200, (-5, 5), 1.0, 3, 0.0, 10),
+                                  ("d14_k127_forced_empty", 100_000, 14, 127, 127, (-10, 10), 1.5, 1,
+                                   0.0, 8, True)])
 @pytest.mark.parametrize("form", sorted(FORMS))
 def test_mixed_driver_tracks_oracle(oracle, case, form):
-    name, n, d, centers, k, box, std, seed, tol, max_iter = case
+    name, n, d, centers, k, box, std, seed, tol, max_iter = case[:10]
+    far = len(case) > 10 and case[10]
     X, _, _ = bench.make_blobs(n, d, centers, box, std, seed)
-    C0 = bench.random_row_init(X, k, seed)
-    it_o, lab_o, C_o, inr_o, _ = oracle.kmeans_lloyd_driver(X, np.ones(n, np.float32), C0, tol, max_iter)
+    C0 = bench.random_row_init(X, k, seed, far_first=far)
+    it_o, lab_o, C_o, inr_o, rel_o = oracle.kmeans_lloyd_driver(X, np.ones(n, np.float32), C0, tol,
+                                                                max_iter)
+    if far:
+        assert rel_o >= 1
     it_g, lab_g, C_g, inr_g, _, total = _fit_labels(X, C0, FORMS[form], max_iter=max_iter, tol=tol)
     assert it_g == it_o
     diff = lab_g != lab_o
@@ -118,16 +126,20 @@ def test_mixed_driver_tracks_oracle(oracle, case, form):
 # update within float32 accumulation tolerance, and the final pass exact.
 @pytest.mark.parametrize("case", [("d64_k256", 60_000, 64, 256, 256, (-5, 5), 1.0, 2, 6),
                                   ("d64_k1024_sigma", 100_000, 64, 1024, 1024, (-5, 5), (0.5, 2.0), 2, 4),
-                                  ("d100_k300", 30_000, 100, 150, 300, (-5, 5), 1.0, 4, 3)])
+                                  ("d100_k300", 30_000, 100, 150, 300, (-5, 5), 1.0, 4, 3),
+                                  ("d64_k256_forced_empty", 60_000, 64, 256, 256, (-5, 5), 1.0, 6, 3,
+                                   True)])
 @pytest.mark.parametrize("form", sorted(FORMS))
 def test_mixed_iterations_match_oracle_step_by_step(oracle, case, form):
     import torch
 
     from kmeans_dpcpp_gb300 import capi
 
-    name, n, d, centers, k, box, std, seed, iters = case
+    name, n, d, centers, k, box, std, seed, iters = case[:9]
+    far = len(case) > 9 and case[9]
     X, _, _ = bench.make_blobs(n, d, centers, box, std, seed)
-    C0 = bench.random_row_init(X, k, seed)
+    C0 = bench.random_row_init(X, k, seed, far_first=far)
+    relocated = 0
     w = np.ones(n, np.float32)
     L = capi.lib()
     Xg = torch.from_numpy(np.ascontiguousarray(X)).cuda()
@@ -146,7 +158,8 @@ def test_mixed_iterations_match_oracle_step_by_step(oracle, case, form):
             capi.check(L.kmc_fit_step(fit, 1))
             stream.synchronize()
             np.testing.assert_array_equal(lab.cpu().numpy(), oracle.assignment(X, C_before))
-            _, _, C_o, _, _ = oracle.kmeans_lloyd_driver(X, w, C_before, 0.0, 1)
+            _, _, C_o, _, rel = oracle.kmeans_lloyd_driver(X, w, C_before, 0.0, 1)
+            relocated += rel
             C_after = cur.cpu().numpy()
             np.testing.assert_allclose(C_after, C_o, rtol=1e-5, atol=1e-5 * np.abs(C_o).max())
         it, inertia = ctypes.c_int64(), ctypes.c_double()
@@ -156,6 +169,8 @@ def test_mixed_iterations_match_oracle_step_by_step(oracle, case, form):
     finally:
         capi.check(L.kmc_fit_destroy(fit))
     assert err.value == 0 and it.value == iters
+    if far:
+        assert relocated >= 1
     C_final = res.cpu().numpy()
     lab_final = lab.cpu().numpy()
     np.testing.assert_array_equal(lab_final, oracle.assignment(X, C_final))
