@@ -209,6 +209,31 @@ def test_driver_parity(kdp, oracle, case, dt):
         assert rel_o >= 1  # the forced empty cluster was relocated
 
 
+def test_driver_full_size_float64_fixed_point(kdp, oracle):
+    """5M x 14, k = 127 in float64 (the at-scale workload, centroid 0 forced empty), tol = 0,
+    max_iter = 100: two runs give the same iteration count and the same bits; labels are the
+    exact argmin against the returned centroids (20k subset); the inertia equals the float64
+    sum of per-sample inertia; and if the fit stopped early, one more iteration from its
+    centroids leaves them unchanged (an exactly zero shift, the reference's stop)."""
+    n, d, k = 5_000_000, 14, 127
+    X, _, _ = bench.make_blobs(n, d, k, (-10, 10), 1.5, 1, dtype=np.float64)
+    C0 = bench.random_row_init(X, k, 1, far_first=True)
+    it, lab, C, inr = _run_driver(kdp, X, C0, 0.0, 100)
+    it2, lab2, C2, inr2 = _run_driver(kdp, X, C0, 0.0, 100)
+    assert it == it2 and inr == inr2
+    np.testing.assert_array_equal(lab, lab2)
+    np.testing.assert_array_equal(C, C2)
+    sub = np.random.default_rng(0).choice(n, 20_000, replace=False)
+    np.testing.assert_array_equal(lab[sub], oracle.assignment(np.ascontiguousarray(X[:, sub]), C))
+    assert np.bincount(lab, minlength=k).sum() == n
+    per = oracle.compute_inertia(X, np.ones(n), C, lab)
+    assert inr == pytest.approx(oracle.sum_ld(per), rel=1e-12)
+    if it < 100:
+        it3, _, C3, _ = _run_driver(kdp, X, C, 0.0, 1)
+        assert it3 == 1
+        np.testing.assert_array_equal(C3, C)
+
+
 def test_driver_float64_reproducible(kdp):
     """float64 fits sum each CTA's samples in a fixed order: two runs of the same fit give
     the same bits, and a zero tolerance stops once the labels settle."""
