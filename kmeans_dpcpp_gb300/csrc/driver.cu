@@ -214,12 +214,10 @@ int PlainFit<T, I>::run(int64_t max_batch) {
 }
 
 template <typename T, typename I>
-int PlainFit<T, I>::finalize(int64_t *n_iter_out, double *inertia_out) {
+int PlainFit<T, I>::finalize_enqueue(LoopState *state_out, double *inertia_out) {
     const FitParams<T, I> &p = prm;
     const int64_t n = p.n, d = p.d, k = p.k;
     cudaStream_t s = p.stream;
-    LoopState h{};
-    KMC_TRY(read_state(h));
     // kmeans_lloyd_driver.hpp:360-418: final assignment and inertia against
     // the final centroids.
     KMC_TRY(launch_half_norm<T>(p.centroids, hn, d, k, s));
@@ -234,9 +232,18 @@ int PlainFit<T, I>::finalize(int64_t *n_iter_out, double *inertia_out) {
     if (p.new_centroids != p.centroids && d * k > 0)
         KMC_CUDA_TRY(cudaMemcpyAsync(p.new_centroids, p.centroids, sizeof(T) * d * k,
                                      cudaMemcpyDeviceToDevice, s));
+    KMC_CUDA_TRY(cudaMemcpyAsync(inertia_out, dsum, sizeof(double), cudaMemcpyDeviceToHost, s));
+    KMC_CUDA_TRY(cudaMemcpyAsync(state_out, state, sizeof(LoopState), cudaMemcpyDeviceToHost, s));
+    return KMC_OK;
+}
+
+template <typename T, typename I>
+int PlainFit<T, I>::finalize(int64_t *n_iter_out, double *inertia_out) {
+    LoopState h{};
     double tot = 0.0;
-    KMC_CUDA_TRY(cudaMemcpyAsync(&tot, dsum, sizeof(double), cudaMemcpyDeviceToHost, s));
-    KMC_CUDA_TRY(cudaStreamSynchronize(s));
+    KMC_TRY(finalize_enqueue(&h, &tot));
+    KMC_CUDA_TRY(cudaStreamSynchronize(prm.stream));
+    host_done = h.done;
     if (n_iter_out) *n_iter_out = h.n_iter;
     if (inertia_out) *inertia_out = tot;
     return KMC_OK;

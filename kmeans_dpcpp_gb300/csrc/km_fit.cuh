@@ -56,7 +56,13 @@ struct FitBase {
     // Enqueue exactly one iteration (no host synchronisation).
     virtual int enqueue_iteration() = 0;
     virtual int read_state(LoopState &out) = 0;
+    // Device copy of the loop state (read by every kernel of an iteration).
+    virtual const LoopState *device_state() const = 0;
     virtual int finalize(int64_t *n_iter_out, double *inertia_out) = 0;
+    // The final pass without host synchronisation: the loop state and the
+    // inertia total land in *state_out and *inertia_out (pinned host memory)
+    // once the fit's stream reaches this point.
+    virtual int finalize_enqueue(LoopState *state_out, double *inertia_out) = 0;
     // Samples re-evaluated in exact arithmetic (mixed form): last pass and total.
     virtual int counters(int64_t *last, int64_t *total, int *device_error) {
         if (last) *last = 0;
@@ -88,6 +94,8 @@ struct PlainFit : FitBase {
     int read_state(LoopState &out) override;
     int run(int64_t max_batch) override;
     int finalize(int64_t *n_iter_out, double *inertia_out) override;
+    int finalize_enqueue(LoopState *state_out, double *inertia_out) override;
+    const LoopState *device_state() const override { return state; }
     // Assignment + accumulation of one iteration (the fused Lloyd step);
     // reports the number of kernels it launched.
     virtual int step_assign_and_accumulate(const T *cur, int64_t *n_launches);

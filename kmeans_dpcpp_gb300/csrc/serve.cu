@@ -505,7 +505,52 @@ struct Active {
     int stream = 0;
     int64_t bytes = 0;
     std::unique_ptr<ReqMem> mem;
+    // mixed fits and predictions: one captured iteration (kernels + a copy of
+    // the loop state to pinned host memory), the event that marks the end of
+    // the session's last enqueued work, and its pinned result slot
+    cudaGraphExec_t iter_graph = nullptr;
+    cudaEvent_t step_ev = nullptr;
+    int slot = -1;
+    LoopState *hstate = nullptr;
+    double *hinertia = nullptr;
+    bool inflight = false;
+    bool final_enqueued = false;
+    ~Active() {
+        if (iter_graph) cudaGraphExecDestroy(iter_graph);
+        if (step_ev) cudaEventDestroy(step_ev);
+    }
 };
+
+// Iterations a mixed session is given per visit of the serving loop: the loop
+// state is checked between visits, and iterations enqueued past the stop are
+// no-ops (every kernel reads the device loop state first).
+constexpr int kItersPerVisit = 4;
+
+// Captures one iteration of a session into a graph, followed by a copy of the
+// loop state into the session's pinned slot.
+int capture_iteration(Active &a) {
+    cudaGraph_t g = nullptr;
+    KMC_CUDA_TRY(cudaStreamBeginCapture(a.st, cudaStreamCaptureModeRelaxed));
+    int rc = a.fit->enqueue_iteration();
+    if (rc == KMC_OK) {
+        const cudaError_t e = cudaMemcpyAsync(a.hstate, a.fit->device_state(), sizeof(LoopState),
+                                              cudaMemcpyDeviceToHost, a.st);
+        if (e != cudaSuccess) {
+            set_error("CUDA error %s in capture_iteration", cudaGetErrorName(e));
+            rc = KMC_ERR_CUDA;
+        }
+    }
+    const cudaError_t ee = cudaStreamEndCapture(a.st, &g);
+    if (rc != KMC_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    KMC_CUDA_TRY(ee);
+    const cudaError_t ei = cudaGraphInstantiate(&a.iter_graph, g, 0);
+    cudaGraphDestroy(g);
+    KMC_CUDA_TRY(ei);
+    return KMC_OK;
+}
 
 int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t budget,
               int64_t max_active, cudaStream_t s, kmc_serve_result_t *out, double *makespan) {
@@ -557,6 +602,23 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
             }
         }
     } pool_guard{pool};
+    // pinned result slots of the mixed sessions (loop state, inertia total)
+    constexpr size_t kSlotBytes = 128;
+    const int64_t n_slots = plain ? 0 : std::max<int64_t>(1, std::min<int64_t>(max_active, n_req));
+    char *pinned = nullptr;
+    std::vector<int> free_slots;
+    if (!plain) {
+        KMC_CUDA_TRY(cudaHostAlloc(&pinned, kSlotBytes * (size_t)n_slots, cudaHostAllocDefault));
+        for (int64_t q = n_slots - 1; q >= 0; --q) free_slots.push_back((int)q);
+    }
+    struct PinnedGuard {
+        char *p;
+        std::vector<cudaStream_t> &streams;
+        ~PinnedGuard() {  // runs before the stream pool is destroyed
+            for (auto t : streams) cudaStreamSynchronize(t);
+            if (p) cudaFreeHost(p);
+        }
+    } pinned_guard{pinned, pool};
 
     std::vector<std::vector<float>> models((size_t)n_req);
     std::vector<char> model_ready((size_t)n_req, 0);
@@ -587,6 +649,10 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
         o.status = status;
         in_use -= a.bytes;
         ++finished;
+        if (a.slot >= 0) {
+            free_slots.push_back(a.slot);
+            a.slot = -1;
+        }
         return KMC_OK;
     };
 
@@ -612,12 +678,15 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
             KMC_CUDA_TRY(cudaMemcpyAsync(idx.ptr, rows.data(), sizeof(int32_t) * rows.size(),
                                          cudaMemcpyHostToDevice, st));
             KMC_TRY(launch_gather_rows(m.X, n, d, idx.as<int32_t>(), k, m.C, st));
-            KMC_CUDA_TRY(cudaStreamSynchronize(st));
+            // (a pageable upload returns once its source is staged, and the
+            // index buffer is freed in stream order: the mixed sessions need
+            // no wait here)
+            if (plain) KMC_CUDA_TRY(cudaStreamSynchronize(st));
         } else {
             const std::vector<float> &mdl = models[(size_t)q.model];
             KMC_CUDA_TRY(cudaMemcpyAsync(m.C, mdl.data(), sizeof(float) * mdl.size(),
                                          cudaMemcpyHostToDevice, st));
-            KMC_CUDA_TRY(cudaStreamSynchronize(st));
+            if (plain) KMC_CUDA_TRY(cudaStreamSynchronize(st));
         }
         out[r].admit_s = elapsed();
         if (plain) {
@@ -649,6 +718,14 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
             p.max_iter = q.kind == 0 ? q.max_iter : 0;
             p.stream = st;
             KMC_TRY(make_mixed_fit<float, int32_t>(p, form, &a->fit));
+            a->slot = free_slots.back();
+            free_slots.pop_back();
+            a->hstate = reinterpret_cast<LoopState *>(pinned + kSlotBytes * (size_t)a->slot);
+            a->hinertia = reinterpret_cast<double *>(pinned + kSlotBytes * (size_t)a->slot + 64);
+            // the slot's previous session has retired: nothing writes it now
+            *reinterpret_cast<volatile int *>(&a->hstate->done) = 0;
+            KMC_CUDA_TRY(cudaEventCreateWithFlags(&a->step_ev, cudaEventDisableTiming));
+            if (p.max_iter > 0) KMC_TRY(capture_iteration(*a));
         }
         in_use += bytes;
         active.push_back(std::move(a));
@@ -710,18 +787,16 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
                 }
             }
         } else {
-            // one iteration of every running session, overlapped across streams
-            std::vector<int> was_done(active.size(), 0);
-            for (size_t t = 0; t < active.size(); ++t) {
-                if (!active[t]->fit) continue;  // a transform in flight
-                LoopState st{};
-                KMC_TRY(active[t]->fit->read_state(st));
-                was_done[t] = st.done;
-                if (!st.done) KMC_TRY(active[t]->fit->enqueue_iteration());
-            }
+            // Each session advances on its own: once its last enqueued work is
+            // done it gets kItersPerVisit more iterations (one graph launch
+            // each) or, when its loop has stopped, the final pass, and it
+            // retires when that is done.  No step waits for the slowest
+            // session, and the host neither launches kernels one by one nor
+            // waits on a stream.
+            bool progressed = false;
             for (size_t t = 0; t < active.size();) {
                 Active &a = *active[t];
-                if (!a.fit) {
+                if (!a.fit) {  // a transform in flight
                     const cudaError_t q = cudaEventQuery(a.ev);
                     if (q == cudaErrorNotReady) {
                         ++t;
@@ -730,22 +805,40 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
                     KMC_CUDA_TRY(q);
                     KMC_TRY(finish(a, 0, 0.0, KMC_OK));
                     active.erase(active.begin() + (int64_t)t);
+                    progressed = true;
                     continue;
                 }
-                LoopState st{};
-                KMC_TRY(a.fit->read_state(st));
-                if (st.done) {
-                    int64_t it = 0;
-                    double inertia = 0.0;
-                    KMC_TRY(a.fit->finalize(&it, &inertia));
-                    KMC_TRY(finish(a, it, inertia, KMC_OK));
+                if (a.inflight) {
+                    const cudaError_t q = cudaEventQuery(a.step_ev);
+                    if (q == cudaErrorNotReady) {
+                        ++t;
+                        continue;
+                    }
+                    KMC_CUDA_TRY(q);
+                    a.inflight = false;
+                }
+                const volatile LoopState *hs = a.hstate;
+                if (a.final_enqueued) {
+                    KMC_TRY(finish(a, (int64_t)hs->n_iter, *(const volatile double *)a.hinertia,
+                                   KMC_OK));
                     a.fit.reset();
                     active.erase(active.begin() + (int64_t)t);
-                } else {
-                    ++t;
+                    progressed = true;
+                    continue;
                 }
+                if (a.iter_graph == nullptr || hs->done) {
+                    KMC_TRY(a.fit->finalize_enqueue(a.hstate, a.hinertia));
+                    a.final_enqueued = true;
+                } else {
+                    for (int r = 0; r < kItersPerVisit; ++r)
+                        KMC_CUDA_TRY(cudaGraphLaunch(a.iter_graph, a.st));
+                }
+                KMC_CUDA_TRY(cudaEventRecord(a.step_ev, a.st));
+                a.inflight = true;
+                progressed = true;
+                ++t;
             }
-            (void)was_done;
+            if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
         }
     }
     if (makespan) *makespan = elapsed();

@@ -263,6 +263,51 @@ def test_serving_loop_matches_requests_served_alone(form):
         assert alone[0].inertia == pytest.approx(mixed[r].inertia, rel=rel)
 
 
+def _served_fit_direct(spec_row, form):
+    """The fit a request describes, run as a direct fit session on the same
+    device-generated blobs and seeded initial rows the serving loop uses."""
+    import torch
+
+    capi, L = _lib()
+    _, kind, n, d, k, seed, tol, mi, _ = spec_row
+    req = _requests([spec_row])[0]
+    s = torch.cuda.current_stream()
+    X = torch.empty((d, n), dtype=torch.float32, device="cuda")
+    capi.check(L.kmc_generate_blobs_f32(X.data_ptr(), n, d, req.n_centers, -10.0, 10.0, req.std_lo,
+                                        req.std_hi, seed, s.cuda_stream))
+    rows = (ctypes.c_int32 * k)()
+    capi.check(L.kmc_seeded_rows(n, k, seed ^ 0x9999, rows))
+    cur = X[:, torch.tensor(list(rows), dtype=torch.int64, device="cuda")].contiguous()
+    res = torch.empty_like(cur)
+    w = torch.ones(n, dtype=torch.float32, device="cuda")
+    lab = torch.empty(n, dtype=torch.int32, device="cuda")
+    fit = ctypes.c_void_p()
+    capi.check(L.kmc_fit_create_f32_i32(X.data_ptr(), w.data_ptr(), cur.data_ptr(), lab.data_ptr(),
+                                        res.data_ptr(), n, d, k, tol, mi, form, s.cuda_stream,
+                                        ctypes.byref(fit)))
+    try:
+        capi.check(L.kmc_fit_run(fit))
+        it, inr = ctypes.c_int64(), ctypes.c_double()
+        capi.check(L.kmc_fit_finalize(fit, ctypes.byref(it), ctypes.byref(inr)))
+    finally:
+        capi.check(L.kmc_fit_destroy(fit))
+    return it.value, inr.value
+
+
+def test_mixed_serving_equals_direct_fit_sessions():
+    """The tensor-core serving sessions (one captured iteration replayed per visit, results
+    read back without host waits) give the fits a direct session gives; up to 32
+    features their sums are float64, so iteration counts match exactly."""
+    mixed, _ = _serve(SPEC, 2)
+    for r, row in enumerate(SPEC):
+        if row[1] != 0 or row[3] > 32:
+            continue
+        it, inr = _served_fit_direct(row, 2)
+        assert mixed[r].status == 0
+        assert mixed[r].n_iter == it, r
+        assert mixed[r].inertia == pytest.approx(inr, rel=1e-6), r
+
+
 def test_serving_admission_respects_the_memory_budget():
     from kmeans_dpcpp_gb300 import capi
 
