@@ -311,8 +311,18 @@ __global__ void batch_reduce_kernel(BInst *tab, const int *idx, int count, int *
     const int d = in.d, k = in.k;
     const int64_t dk = (int64_t)d * k;
     for (int64_t e = threadIdx.x; e < dk + k; e += blockDim.x) {
+        // copies added in index order; loads issued eight ahead of the adds
+        const double *src = in.sums + e;
         double s = 0.0;
-        for (int c = 0; c < in.copies; ++c) s += in.sums[(int64_t)c * (dk + k) + e];
+        int c = 0;
+        for (; c + 8 <= in.copies; c += 8) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = src[(int64_t)(c + u) * (dk + k)];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += v[u];
+        }
+        for (; c < in.copies; ++c) s += src[(int64_t)c * (dk + k)];
         if (e < dk)
             in.Cn[e] = (float)s;
         else

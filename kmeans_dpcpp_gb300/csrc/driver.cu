@@ -37,7 +37,9 @@ int PlainFit<T, I>::init(const FitParams<T, I> &p) {
     // float64 atomics would be compare-and-swap loops on the critical path.
     // float64 samples get a copy per CTA up to 256 MiB of copies: each CTA
     // then sums its samples in a fixed order (bit-reproducible centroids).
-    if (sizeof(T) == 8) {
+    if (!uses_private_copies()) {
+        P = 1;
+    } else if (sizeof(T) == 8) {
         const int64_t per_copy = 8 * (d + 1) * std::max<int64_t>(k, 1);
         P = std::max<int64_t>(1, std::min<int64_t>(2 * (int64_t)num_sms(),
                                                    (int64_t(256) << 20) / per_copy));
@@ -123,8 +125,11 @@ int PlainFit<T, I>::enqueue_iteration() {
     x_view(&xv, &xfs, &xss);
     // kmeans_lloyd_driver.hpp:86-111
     KMC_TRY(launch_half_norm<T>(cur, hn, d, k, s, state));
-    KMC_TRY(launch_fill<double>(sums_cp, 0.0, P * d * k, s, state));
-    KMC_TRY(launch_fill<double>(sizes_cp, 0.0, P * k, s, state));
+    const bool copies = uses_private_copies();
+    if (copies) {
+        KMC_TRY(launch_fill<double>(sums_cp, 0.0, P * d * k, s, state));
+        KMC_TRY(launch_fill<double>(sizes_cp, 0.0, P * k, s, state));
+    }
     KMC_TRY(launch_fill<I>(n_empty, I(0), 1, s, state));
     // kmeans_lloyd_driver.hpp:124-143
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -166,7 +171,8 @@ int PlainFit<T, I>::enqueue_iteration() {
     KMC_CUDA_TRY(cudaMemcpyAsync(cur, nxt, sizeof(T) * d * k, cudaMemcpyDeviceToDevice, s));
     // 4 (norm, fills) + step + 2 (reduce) + gate + inertia + threshold + 2 fills
     // + 4 (select) + relocate + divide/shift + control
-    launches += 4 + step_launches + 2 + verbose_launches + 1 + 1 + thr_launches + 2 + 4 + 1 + 1 + 1;
+    launches += (copies ? 4 : 2) + step_launches + 2 + verbose_launches + 1 + 1 + thr_launches + 2 +
+                4 + 1 + 1 + 1;
     ++issued;
     return KMC_OK;
 }

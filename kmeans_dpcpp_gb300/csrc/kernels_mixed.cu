@@ -1059,8 +1059,17 @@ __global__ void km_to_dk_kernel(const A *copies, int n_copies, float *out_c, flo
         const int64_t off = is_size ? k_pad * d4 + (e - k * d4) : e;
         const int64_t j = e / d4, f = e % d4;
         if (!is_size && f >= d) continue;
+        // copies added in index order; loads issued eight ahead of the adds
         double acc = 0.0;
-        for (int c = 0; c < n_copies; ++c) acc += (double)copies[(int64_t)c * cs + off];
+        int c = 0;
+        for (; c + 8 <= n_copies; c += 8) {
+            A v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = copies[(int64_t)(c + u) * cs + off];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) acc += (double)v[u];
+        }
+        for (; c < n_copies; ++c) acc += (double)copies[(int64_t)c * cs + off];
         if (is_size)
             out_sizes[e - k * d4] = (float)acc;
         else
@@ -1141,6 +1150,7 @@ struct MixedFit : PlainFit<float, I> {
     // The one-time conversion reads X in either layout; afterwards every
     // kernel reads the row-major fp32 copy.
     bool reads_rowmajor() const override { return true; }
+    bool uses_private_copies() const override { return false; }
     void x_view(const float **x, int64_t *fs, int64_t *ss) const override {
         *x = xrow;
         *fs = 1;
@@ -1189,12 +1199,15 @@ struct MixedFit : PlainFit<float, I> {
         const size_t o_ct = take(sizeof(float) * k_pad * d4);
         const size_t o_nx = take(sizeof(float) * p.n);
         const size_t o_ndx = take(sizeof(float) * p.n);
-        // Small sums get one private copy per CTA of the assignment: their
-        // few addresses would otherwise serialise the reductions of all SMs.
-        // Large ones (c3-sized, 266 KB) stay single: per-CTA copies would
+        // Small sums get private copies, one per CTA of the assignment for
+        // large n: their few addresses would otherwise serialise the
+        // reductions of all SMs.  Every iteration zeroes and reduces every
+        // copy, so small fits get one copy per eight tiles instead (a
+        // 50K-sample fit spent more time there than in its assignment).
+        // Large sums (c3-sized, 266 KB) stay single: per-CTA copies would
         // crowd L2 for less contention than they remove.
         n_copies = (k_pad * d4 <= 32768)
-                       ? (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, num_sms()))
+                       ? (int)std::max<int64_t>(1, std::min<int64_t>(ntiles / 8, num_sms()))
                        : 1;
         const int64_t csz = (int64_t)n_copies * (k_pad * d4 + k_pad);
         const size_t o_s32 = take(acc_f64 ? 16 : sizeof(float) * csz);
@@ -1312,7 +1325,11 @@ struct MixedFit : PlainFit<float, I> {
             kern<<<(unsigned)grid, kThreadsMixed, L.total, s>>>(a);
             KMC_TRY(check_launch("mixed_assign"));
         }
-        recheck_kernel<<<(unsigned)(num_sms() * 8), kRecheckThreads, 0, s>>>(
+        // enough CTAs for every sample flagged (8 warps of 32 per CTA round),
+        // at most 8 per SM
+        const int64_t rgrid = std::max<int64_t>(
+            1, std::min<int64_t>((int64_t)num_sms() * 8, ceil_div<int64_t>(p.n, kRecheckThreads)));
+        recheck_kernel<<<(unsigned)rgrid, kRecheckThreads, 0, s>>>(
             xrow, ct, this->hn, p.w, cand, flagged, n_flagged, p.n, p.d, p.k, d4, p.labels,
             a.label64, update, acc_f64, sums32, acc64, k_pad, n_copies, guard);
         KMC_TRY(check_launch("mixed_recheck"));

@@ -58,16 +58,23 @@ __global__ void reduce_copies_kernel(const A *sizes_cp, const A *cent_cp, T *out
     int64_t dk = d * k;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < dk + k;
          e += (int64_t)gridDim.x * blockDim.x) {
-        if (e < dk) {
-            A s = A(0);
-            for (int64_t p = 0; p < P; ++p) s += cent_cp[p * dk + e];
-            out_cent[e] = (T)s;
-        } else {
-            int64_t j = e - dk;
-            A s = A(0);
-            for (int64_t p = 0; p < P; ++p) s += sizes_cp[p * k + j];
-            out_sizes[j] = (T)s;
+        // copies added in index order; loads issued eight ahead of the adds
+        const A *src = (e < dk) ? cent_cp + e : sizes_cp + (e - dk);
+        const int64_t stride = (e < dk) ? dk : k;
+        A s = A(0);
+        int64_t p = 0;
+        for (; p + 8 <= P; p += 8) {
+            A v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = src[(p + u) * stride];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += v[u];
         }
+        for (; p < P; ++p) s += src[p * stride];
+        if (e < dk)
+            out_cent[e] = (T)s;
+        else
+            out_sizes[e - dk] = (T)s;
     }
 }
 

@@ -104,6 +104,9 @@ struct PlainFit : FitBase {
     // Private copies -> new centroid sums, sizes and the empty-cluster list
     // (kmeans_lloyd_driver.hpp:155-170).
     virtual int reduce_step(T *nxt);
+    // Whether the step accumulates into the driver's float64 private copies
+    // (the mixed forms keep their own sums).
+    virtual bool uses_private_copies() const { return true; }
     // Whether the form reads a row-major X itself (else init makes a
     // feature-major copy).
     virtual bool reads_rowmajor() const { return false; }
