@@ -563,12 +563,14 @@ int kmc_seeded_rows(int64_t n_samples, int64_t n_clusters, uint64_t seed, int32_
  * No counterpart in the reference.  Replays a stream of fit and predict
  * requests against the engine with continuous batching: a request is
  * admitted at its arrival time as soon as an instance slot is free and the
- * device bytes it needs fit the budget; running fits advance together one
- * iteration per step; converged fits retire mid-batch and free their memory.
+ * device bytes it needs fit the budget; running fits advance concurrently
+ * (in the plain form together, one iteration per engine step); converged fits
+ * retire mid-batch and free their memory.
  * Each request's data are seeded Gaussian blobs generated on the device at
  * admission.  form KMC_FORM_PLAIN runs the batched engine; the mixed forms run
- * one tensor-core fit session per request on a pool of streams.  Times are
- * seconds from the start of the replay. */
+ * one tensor-core fit session per request on a pool of streams, each session
+ * replaying one captured iteration (a CUDA graph) and advancing on its own.
+ * Times are seconds from the start of the replay. */
 typedef struct {
     double arrival_s;
     int32_t kind;        /* 0 fit, 1 predict, 2 transform (distances; result.inertia = their float64 sum) */
