@@ -1040,7 +1040,7 @@ __global__ void __launch_bounds__(kRecheckThreads) recheck_kernel(
                 }
             }
         }
-        __syncwarp();  // the keys and masks of this round are read before the next one
+        __syncwarp();  // this batch's keys and masks are read before the next batch
     }
 }
 
