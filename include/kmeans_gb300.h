@@ -511,8 +511,8 @@ int kmc_kmeans_plusplus_f64(const double *X_t, const double *sample_weight, int6
                             double *centroids_t, int32_t *chosen_rows, kmc_stream_t stream);
 
 /* ---- batched fits ------------------------------------------------------------------
- * No counterpart in the reference.  Many independent float32 fits and label-only predictions of uneven
- * (n, d, k) advance together, one Lloyd iteration per kmc_batch_step, through
+ * No counterpart in the reference.  Many independent float32 fits and
+ * label-only predictions of uneven (n, d, k) advance together, one Lloyd iteration per kmc_batch_step, through
  * per-phase kernels fed by a device work queue and replayed as CUDA graphs.
  * Each fit follows kmeans_lloyd_driver's semantics (stop rule, empty-cluster
  * relocation, final assignment and inertia) with the plain form's arithmetic:
