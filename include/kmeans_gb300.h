@@ -512,8 +512,9 @@ int kmc_kmeans_plusplus_f64(const double *X_t, const double *sample_weight, int6
 
 /* ---- batched fits ------------------------------------------------------------------
  * No counterpart in the reference.  Many independent float32 fits and
- * label-only predictions of uneven (n, d, k) advance together, one Lloyd iteration per kmc_batch_step, through
- * per-phase kernels fed by a device work queue and replayed as CUDA graphs.
+ * label-only predictions of uneven (n, d, k) advance together, one Lloyd
+ * iteration per kmc_batch_step, through per-phase kernels fed by a device work
+ * queue and replayed as CUDA graphs.
  * Each fit follows kmeans_lloyd_driver's semantics (stop rule, empty-cluster
  * relocation, final assignment and inertia) with the plain form's arithmetic:
  * labels equal a single plain fit's, centroids and inertia agree to float64
