@@ -50,6 +50,15 @@ int kmc_abi_version(void);
  * of mapping it again (~9 ms per 4 GB).  This returns the pool's unused memory
  * on every device to the system; memory of live fits is unaffected. */
 int kmc_trim_cached_memory(void);
+/* No counterpart in the reference.  Bytes of that pool in use by live work
+ * on the current device (memory that is mapped but free is not counted). */
+int kmc_scratch_bytes_in_use(int64_t *bytes_out);
+/* No counterpart in the reference; a test hook of the out-of-memory paths.
+ * After this call the (after + 1)-th scratch allocation of the library (any
+ * thread, any device) fails as the device's allocator does when memory runs
+ * out: the call that asked for it releases what it had taken and returns
+ * KMC_ERR_OUT_OF_MEMORY.  The hook fires once; after < 0 disarms it. */
+int kmc_debug_fail_allocation(int64_t after);
 
 /* ---- broadcast_divide: X /= y column-wise --------------------------------
  * replaces py_broadcast_divide (_kmeans_lloyd.cpp:60-105) ->
@@ -164,7 +173,9 @@ int kmc_select_samples_far_from_centroid_f64_i64(int64_t n_selected,
  * cudaMalloc / cudaFree or other allocating call.  Calls whose kernels overlap
  * on the same device (other streams or host threads) race on the shared
  * scratch.  The first call on a device looks the array up with
- * cudaGetSymbolAddress; make it before any stream capture. */
+ * cudaGetSymbolAddress; make it before any stream capture.  The address is
+ * kept per device and context, so after a device reset the next call looks
+ * it up again (again before any capture). */
 int kmc_select_samples_far_from_centroid_noalloc_f32_i32(int64_t n_selected,
                                                          const float *distance_to_centroid,
                                                          const float *threshold,
@@ -474,6 +485,18 @@ int kmc_fit_phase_time(kmc_fit_t fit, int phase, double *total_ms_out, int64_t *
  * the device-side error flag of the tensor-core kernel (1 after a bounded
  * wait timed out).  Plain form: zeros.  Blocking. */
 int kmc_fit_rechecked(kmc_fit_t fit, int64_t *last_out, int64_t *total_out, int *device_error_out);
+/* No counterpart in the reference.  Limit, in SM clocks, of every
+ * device-side wait of the tensor-core kernels of a mixed-form session
+ * (clocks <= 0 restores the default, 4e9 clocks or about two seconds).  A
+ * wait that runs out makes the kernel wind down (it waits for the copies and
+ * tensor-core operations it issued, frees its tensor memory) and stops the
+ * loop; the next blocking call (kmc_fit_run, kmc_fit_status,
+ * kmc_fit_finalize) returns KMC_ERR_DEVICE_TIMEOUT and kmc_fit_rechecked
+ * reports device_error = 1.  stall_once = 1 makes the next assignment pass
+ * first wait on a barrier that nothing completes, so that this wait runs out
+ * after `clocks`: a test of the timeout path that faults and hangs nothing.
+ * The plain form has no device-side waits and ignores both. */
+int kmc_fit_set_wait_limit(kmc_fit_t fit, int64_t clocks, int stall_once);
 /* Kernel launches enqueued so far by this session. */
 int kmc_fit_launch_count(kmc_fit_t fit, int64_t *launches_out);
 int kmc_fit_destroy(kmc_fit_t fit);

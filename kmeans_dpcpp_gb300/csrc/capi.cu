@@ -26,6 +26,8 @@ void set_error(const char *fmt, ...) {
 
 const char *get_error() { return g_err; }
 
+std::atomic<long long> g_fail_alloc_after{-1};
+
 int num_sms() {
     static int cache[64] = {0};
     int dev = 0;
@@ -133,7 +135,7 @@ int select_far(int64_t n_sel, const T *dist, const T *thr, I *sel, I *n_gt, I *n
     KMC_CHECK_ARG(n_sel <= n, "Argument `n_select` is too large");
     Scratch sc;
     KMC_TRY(sc.alloc(select_scratch_bytes(n_sel), s));
-    return launch_select<T, I>(nullptr, n_sel, dist, thr, sel, n_gt, n_eq, n, sc.ptr, s);
+    return launch_select<T, I>(nullptr, n_sel, dist, thr, sel, n_gt, n_eq, n, sc.ptr, n_sel, s);
 }
 
 template <typename T, typename I>
@@ -159,7 +161,7 @@ int relocate(int64_t n_empty, const T *X, const T *w, const I *labels, const I *
     KMC_TRY(launch_fill<I>(cnt, I(0), 1, s));
     KMC_TRY(launch_fill<I>(cnt + 1, I(1), 1, s));
     KMC_TRY(launch_select<T, I>(nullptr, n_empty, sq_dist, thr, sel, cnt, cnt + 1, n, b + o_ssc,
-                                s));
+                                n_empty, s));
     return launch_relocate<T, I>(nullptr, n_empty, X, w, labels, sel, cnt, list, C, sizes,
                                  inertia, n, d, k, s);
 }
@@ -305,6 +307,22 @@ extern "C" {
 const char *kmc_last_error(void) { return kmc::get_error(); }
 int kmc_abi_version(void) { return 1; }
 int kmc_trim_cached_memory(void) { return kmc::trim_pools(); }
+
+int kmc_scratch_bytes_in_use(int64_t *bytes_out) {
+    KMC_CHECK_ARG(bytes_out != nullptr, "null output pointer");
+    *bytes_out = 0;
+    cudaMemPool_t pool = kmc::scratch_pool();
+    if (pool == nullptr) return KMC_OK;
+    unsigned long long used = 0;  // the attribute is a 64-bit unsigned value
+    KMC_CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used));
+    *bytes_out = (int64_t)used;
+    return KMC_OK;
+}
+
+int kmc_debug_fail_allocation(int64_t after) {
+    kmc::g_fail_alloc_after.store(after < 0 ? -1 : after);
+    return KMC_OK;
+}
 
 #define KMC_T_ENTRY(SUF, T)                                                                    \
     int kmc_broadcast_divide_##SUF(T *X, const T *y, int64_t r, int64_t c, int64_t,            \
@@ -465,6 +483,10 @@ int kmc_fit_phase_time(kmc_fit_t fit, int phase, double *total_ms, int64_t *coun
 int kmc_fit_rechecked(kmc_fit_t fit, int64_t *last, int64_t *total, int *device_error) {
     KMC_FIT_CHECK(fit);
     return fit->impl->counters(last, total, device_error);
+}
+int kmc_fit_set_wait_limit(kmc_fit_t fit, int64_t clocks, int stall_once) {
+    KMC_FIT_CHECK(fit);
+    return fit->impl->set_wait_limit((long long)clocks, stall_once);
 }
 int kmc_fit_launch_count(kmc_fit_t fit, int64_t *out) {
     KMC_FIT_CHECK(fit);

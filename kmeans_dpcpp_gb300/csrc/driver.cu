@@ -162,7 +162,7 @@ int PlainFit<T, I>::enqueue_iteration() {
     KMC_TRY(launch_fill<I>(counters, I(0), 1, s, state));
     KMC_TRY(launch_fill<I>(counters + 1, I(1), 1, s, state));
     KMC_TRY(launch_select<T, I>(gate, 0, sq_dist, threshold, selected, counters, counters + 1, n,
-                                sel_scratch, s, state));
+                                sel_scratch, k, s, state));
     KMC_TRY(launch_relocate<T, I>(gate, 0, xv, p.w, p.labels, selected, counters, empty_list,
                                   nxt, sizes, sq_dist, n, d, k, s, state, xfs, xss));
     // kmeans_lloyd_driver.hpp:317-353
@@ -172,7 +172,7 @@ int PlainFit<T, I>::enqueue_iteration() {
     // 4 (norm, fills) + step + 2 (reduce) + gate + inertia + threshold + 2 fills
     // + 4 (select) + relocate + divide/shift + control
     launches += (copies ? 4 : 2) + step_launches + 2 + verbose_launches + 1 + 1 + thr_launches + 2 +
-                4 + 1 + 1 + 1;
+                select_launches(k) + 1 + 1 + 1;
     ++issued;
     return KMC_OK;
 }
@@ -191,7 +191,7 @@ int PlainFit<T, I>::read_state(LoopState &out) {
                                  prm.stream));
     KMC_CUDA_TRY(cudaStreamSynchronize(prm.stream));
     host_done = out.done;
-    return KMC_OK;
+    return check_device_error(out);
 }
 
 template <typename T, typename I>
@@ -250,6 +250,7 @@ int PlainFit<T, I>::finalize(int64_t *n_iter_out, double *inertia_out) {
     KMC_TRY(finalize_enqueue(&h, &tot));
     KMC_CUDA_TRY(cudaStreamSynchronize(prm.stream));
     host_done = h.done;
+    KMC_TRY(check_device_error(h));
     if (n_iter_out) *n_iter_out = h.n_iter;
     if (inertia_out) *inertia_out = tot;
     return KMC_OK;

@@ -50,11 +50,19 @@
 //   warp 1      TMEM allocation; one thread issues tcgen05.mma (M=128, N=256,
 //               K=16) into two 256-column TMEM accumulators
 //   warps 2-9   epilogue: tcgen05.ld of score pairs, P1/P2, certification, labels
-//   warps 10-11 update: w*x of certified samples into the cluster sums
-//               (exact int64 fixed-point sums in shared memory flushed once
-//               per CTA when they fit, else red.global.add.v4.f32 into
-//               cluster-major fp32 sums)
+//   warps 10-11 update: w*x of certified samples into cluster-major sums in
+//               global memory, with fire-and-forget reductions
+//               (red.global.add.v4.f32, or red.global.add.f64 per feature
+//               when d <= 32) into the private copy of this CTA (copy
+//               blockIdx % n_copies), summed in copy order afterwards
 // Samples that fail certification are accumulated by the recheck kernel.
+//
+// Every wait is bounded.  A wait that runs out raises the CTA's error flag;
+// the other roles see it and stop, the producer and the MMA issuer then wait
+// (ignoring the flag) for the copies and tensor-core operations they already
+// issued, TMEM is freed, and the fit's loop state records the error and stops
+// the loop, so the host gets KMC_ERR_DEVICE_TIMEOUT and the context stays
+// usable.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -117,6 +125,10 @@ struct MixedArgs {
     int label64;
     int acc_f64;       // red.global.add.f64 per feature (else red.global.add.v4.f32)
     int stages;        // depth of the X-tile ring
+    long long wait_limit;  // SM clocks after which a wait gives up
+    int stall;         // test of the timeout path: the epilogue first waits on a
+                       // barrier that nothing completes
+    LoopState *state;  // receives the error bit and stops the loop (nullable)
 };
 
 struct SmemLayout {
@@ -155,7 +167,7 @@ __host__ __device__ inline SmemLayout smem_layout(int nkb, int64_t k_pad, int64_
     off += sizeof(int) * 2 * kTileM;
     off = (off + 15) & ~size_t(15);
     L.bar = off;
-    off += 8 * 18 + 16;
+    off += 8 * 19 + 16;
     off = (off + 15) & ~size_t(15);
     L.p1 = off;
     if (p1_in_smem(k_pad / kChunkN)) off += sizeof(float) * 32 * kEpiWarps * (size_t)(k_pad / 64);
@@ -257,11 +269,13 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.bar);
     uint64_t *full = bars, *empty = bars + 4, *tfull = bars + 8, *tempty = bars + 10;
     uint64_t *ufull = bars + 12, *uempty = bars + 14, *cbar = bars + 16, *tdone = bars + 17;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 18);
+    uint64_t *never = bars + 18;  // completed by no role (timeout test only)
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 19);
     volatile int *err = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t n = a.n, k = a.k;
+    const long long lim = a.wait_limit;
     const int64_t ntiles = ceil_div<int64_t>(n, kTileM);
     const uint32_t cbytes = (uint32_t)cimg_bytes(NKB, k_pad);
 
@@ -278,6 +292,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
         }
         mbar_init(cbar, 1);
         mbar_init(tdone, 1);
+        mbar_init(never, 1);
         *err = 0;
         fence_barrier_init();
     }
@@ -310,7 +325,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
             int s = 0;
             uint32_t ph = 0, issued = 0u, last_ph = 0u;
             for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-                if (!mbar_wait(&empty[s], ph ^ 1u, err)) break;
+                if (!mbar_wait(&empty[s], ph ^ 1u, err, lim)) break;
                 mbar_arrive_expect_tx(&full[s], NKB * kTileBytes);
                 bulk_g2s(xring + (size_t)s * NKB * kTileBytes,
                          a.ximg + (size_t)tile * NKB * kTileBytes, NKB * kTileBytes, &full[s]);
@@ -321,10 +336,13 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                     ph ^= 1u;
                 }
             }
-            // never leave a copy in flight into this CTA's shared memory
-            mbar_wait(cbar, 0, err);
+            // never leave a copy in flight into this CTA's shared memory: the
+            // centroid image and the last copy into each ring stage (a stage
+            // holds at most one copy in flight) are waited for even after an
+            // error
+            mbar_wait_drain(cbar, 0, err);
             for (int q = 0; q < stages; ++q)
-                if ((issued >> q) & 1u) mbar_wait(&full[q], (last_ph >> q) & 1u, err);
+                if ((issued >> q) & 1u) mbar_wait_drain(&full[q], (last_ph >> q) & 1u, err);
         }
         __syncwarp();
     } else if (warp == 1) {
@@ -334,16 +352,16 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
             const uint32_t cbase = smem_u32(cimg_s);
             const uint32_t hbase = cbase + (uint32_t)(NKB * k_pad * 128);
             const uint64_t adesc_norm = desc_sw32(smem_u32(aon_s));
-            bool ok = mbar_wait(cbar, 0, err);
+            bool ok = mbar_wait(cbar, 0, err, lim);
             int s = 0;
             uint32_t ph = 0, cnt = 0;
             for (int64_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-                if (!mbar_wait(&full[s], ph, err)) break;
+                if (!mbar_wait(&full[s], ph, err, lim)) break;
                 tc_fence_after();
                 const uint32_t xbase = smem_u32(xring + (size_t)s * NKB * kTileBytes);
                 for (int c = 0; c < NCH; ++c) {
                     const uint32_t b = cnt & 1u, bph = (cnt >> 1) & 1u;
-                    if (!mbar_wait(&tempty[b], bph ^ 1u, err)) {
+                    if (!mbar_wait(&tempty[b], bph ^ 1u, err, lim)) {
                         ok = false;
                         break;
                     }
@@ -370,9 +388,10 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                     ph ^= 1u;
                 }
             }
-            // all issued MMAs must have finished before TMEM is released
+            // all issued MMAs must have finished before TMEM is released,
+            // error or not
             mma_commit(tdone);
-            mbar_wait(tdone, 0, err);
+            mbar_wait_drain(tdone, 0, err);
         }
         __syncwarp();
     } else if (warp < 2 + kEpiWarps) {
@@ -392,6 +411,8 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
         const uint32_t lane_addr = (uint32_t)(32 * q) << 16;
         uint32_t cnt = 0;
         int tl = 0;
+        // test of the timeout path: this wait runs out after `lim` clocks
+        if (a.stall) mbar_wait(never, 0, err, lim);
         // per-sample norms of the next tile are loaded one tile ahead
         float nx_next = 0.f, dx_next = 0.f;
         {
@@ -432,7 +453,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
 #pragma unroll kChunkUnroll
             for (int c = 0; c < NCH; ++c) {
                 const uint32_t b = cnt & 1u, bph = (cnt >> 1) & 1u;
-                if (!mbar_wait(&tfull[b], bph, err)) bad = true;
+                if (!mbar_wait(&tfull[b], bph, err, lim)) bad = true;
                 // tcgen05.ld is warp-collective: re-converge after the spin-wait
                 if (__any_sync(0xffffffffu, bad)) {
                     bad = true;
@@ -536,7 +557,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                 }
             }
             const int tb = tl & 1;
-            if (mbar_wait(&uempty[tb], (((uint32_t)tl >> 1) & 1u) ^ 1u, err) && win) {
+            if (mbar_wait(&uempty[tb], (((uint32_t)tl >> 1) & 1u) ^ 1u, err, lim) && win) {
                 lab_s[tb * kTileM + row] = code;
                 mbar_arrive(&ufull[tb]);
             }
@@ -603,7 +624,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                     xb[g] = (a.update && in && i1 < n) ? __ldg(rb + g) : make_float4(0.f, 0.f, 0.f, 0.f);
                 }
                 if (!have_code) {
-                    if (!mbar_wait(&ufull[tb], ((uint32_t)tl >> 1) & 1u, err)) break;
+                    if (!mbar_wait(&ufull[tb], ((uint32_t)tl >> 1) & 1u, err, lim)) break;
                     c0 = lab_s[tb * kTileM + u];
                     c1 = lab_s[tb * kTileM + u + 64];
                     mbar_arrive(&uempty[tb]);
@@ -622,7 +643,14 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
         tc_fence_after();
         tmem_dealloc(tmem, 512);
     }
-    if (threadIdx.x == 0 && *err) atomicExch(a.err_global, 1);
+    if (threadIdx.x == 0 && *err) {
+        atomicExch(a.err_global, 1);
+        if (a.state != nullptr) {
+            // the remaining kernels of the iteration and the host loop stop
+            atomicOr(&a.state->err, 1u);
+            atomicExch(&a.state->done, 1);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1146,6 +1174,14 @@ struct MixedFit : PlainFit<float, I> {
     uint4 *cand = nullptr;
     int *flagged = nullptr, *n_flagged = nullptr, *err_dev = nullptr;
     long long *stats = nullptr;  // [0] last pass, [1] total
+    long long wait_limit = kWaitClocks;
+    int stall_once = 0;
+
+    int set_wait_limit(long long clocks, int stall) override {
+        wait_limit = clocks > 0 ? clocks : kWaitClocks;
+        stall_once = stall != 0;
+        return KMC_OK;
+    }
 
     // The one-time conversion reads X in either layout; afterwards every
     // kernel reads the row-major fp32 copy.
@@ -1311,6 +1347,10 @@ struct MixedFit : PlainFit<float, I> {
         a.label64 = sizeof(I) == 8 ? 1 : 0;
         a.acc_f64 = acc_f64;
         a.stages = stages;
+        a.wait_limit = wait_limit;
+        a.stall = stall_once;
+        a.state = this->state;
+        stall_once = 0;
         const SmemLayout L = smem_layout(nkb, k_pad, d4, stages);
         auto kern = pick_kernel(bf16, nkb, (int)(k_pad / kChunkN));
         if (kern == nullptr) {

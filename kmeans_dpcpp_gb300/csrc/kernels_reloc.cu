@@ -148,13 +148,18 @@ struct SelHeader {
     long long n_total;
 };
 
+// Up to this many selections the strictly-greater samples (fewer than
+// n_selected) are ranked by counting all pairs; beyond it by a merge sort.
+constexpr int64_t kRankAllPairs = 4096;
+
 struct SelLayout {
     SelHeader *hdr;
     long long *cnt_gt, *cnt_eq;  // [kSelGrid]
     long long *gt_list;          // [max_selected] indices, used when ranking
+    long long *gt_tmp;           // [max_selected] second merge buffer (max_selected > kRankAllPairs)
 };
 
-__host__ __device__ inline SelLayout sel_layout(void *base) {
+__host__ __device__ inline SelLayout sel_layout(void *base, int64_t max_selected) {
     char *p = static_cast<char *>(base);
     SelLayout L;
     L.hdr = reinterpret_cast<SelHeader *>(p);
@@ -164,6 +169,7 @@ __host__ __device__ inline SelLayout sel_layout(void *base) {
     L.cnt_eq = reinterpret_cast<long long *>(p);
     p += sizeof(long long) * kSelGrid;
     L.gt_list = reinterpret_cast<long long *>(p);
+    L.gt_tmp = L.gt_list + (max_selected > 0 ? max_selected : 1);
     return L;
 }
 
@@ -306,9 +312,9 @@ __global__ void select_write_kernel(const T *dist, const T *thr, int64_t n, SelL
     }
 }
 
-// Ranks the (at most n_sel - 1) strictly-greater samples by (distance desc,
-// index asc) and stores them so that selected[gt_init + m - 1 - r] holds the
-// r-th farthest.
+// Ranks the (at most n_sel - 1 <= kRankAllPairs) strictly-greater samples by
+// (distance desc, index asc), counting all pairs, and stores them so that
+// selected[gt_init + m - 1 - r] holds the r-th farthest.
 template <typename T, typename I>
 __global__ void select_rank_kernel(const T *dist, SelLayout L, I *selected) {
     const SelHeader *h = L.hdr;
@@ -326,6 +332,75 @@ __global__ void select_rank_kernel(const T *dist, SelLayout L, I *selected) {
         }
         long long pos = h->gt_init + m - 1 - r;
         if (pos >= 0 && pos < h->n_total) selected[pos] = (I)ie;
+    }
+}
+
+// Sample a comes before sample b in the selection order: farther first,
+// the lower index on equal distances (a strict total order: indices differ).
+template <typename T>
+__device__ __forceinline__ bool sel_before(const T *dist, long long a, long long b) {
+    const T va = dist[a], vb = dist[b];
+    return va > vb || (va == vb && a < b);
+}
+
+// Number of entries of the sorted run r[0, len) that come before sample e.
+template <typename T>
+__device__ __forceinline__ long long count_before(const T *dist, const long long *r, long long len,
+                                                  long long e) {
+    long long lo = 0, hi = len;
+    while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (sel_before(dist, r[mid], e)) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// One pass of the merge sort of the m strictly-greater samples (more than
+// kRankAllPairs selections): runs of `len` sorted entries of src are merged
+// pairwise into dst.  An entry's place in the merged run is its place in its
+// own run plus the number of entries of the partner run before it, found by
+// binary search (O(m log len) per pass).  gt_list holds the samples in
+// ascending index order initially, so the first pass starts from runs of 1.
+// A pass whose runs already cover all m entries does nothing.
+template <typename T>
+__global__ void select_merge_kernel(const T *dist, SelLayout L, int pass) {
+    const SelHeader *h = L.hdr;
+    if (h->active == 0 || h->sorted == 0) return;
+    const long long m = h->total_gt, len = 1ll << pass;
+    if (len >= m) return;
+    const long long *src = (pass & 1) ? L.gt_tmp : L.gt_list;
+    long long *dst = (pass & 1) ? L.gt_list : L.gt_tmp;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long base = (e / (2 * len)) * (2 * len);
+        const long long a_len = (m - base < len) ? (m - base) : len;
+        const long long b0 = base + a_len;
+        const long long b_len = (m - b0 < len) ? (m - b0) : len;
+        const long long v = src[e];
+        long long pos;
+        if (e < b0)
+            pos = e + count_before(dist, src + b0, b_len, v);
+        else
+            pos = base + count_before(dist, src + base, a_len, v) + (e - b0);
+        dst[pos] = v;
+    }
+}
+
+// After the merge passes: the sorted list (in the buffer the last effective
+// pass wrote) goes to selected[gt_init + m - 1 - r] for the r-th farthest.
+template <typename T, typename I>
+__global__ void select_place_kernel(SelLayout L, I *selected) {
+    const SelHeader *h = L.hdr;
+    if (h->active == 0 || h->sorted == 0) return;
+    const long long m = h->total_gt;
+    int passes = 0;
+    while ((1ll << passes) < m) ++passes;
+    const long long *srt = (passes & 1) ? L.gt_tmp : L.gt_list;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < m;
+         r += (long long)gridDim.x * blockDim.x) {
+        const long long pos = h->gt_init + m - 1 - r;
+        if (pos >= 0 && pos < h->n_total) selected[pos] = (I)srt[r];
     }
 }
 
@@ -392,15 +467,23 @@ int launch_threshold(const T *data, int64_t n, const int64_t *topk_dev, int64_t 
 }
 
 size_t select_scratch_bytes(int64_t max_selected) {
-    return align256(256 + 2 * sizeof(long long) * kSelGrid +
-                    sizeof(long long) * (size_t)(max_selected > 0 ? max_selected : 1));
+    const size_t m = (size_t)(max_selected > 0 ? max_selected : 1);
+    const size_t lists = (max_selected > kRankAllPairs) ? 2 : 1;
+    return align256(256 + 2 * sizeof(long long) * kSelGrid + sizeof(long long) * m * lists);
+}
+
+int64_t select_launches(int64_t max_selected) {
+    if (max_selected <= kRankAllPairs) return 4;
+    int64_t passes = 0;
+    while ((int64_t(1) << passes) < max_selected) ++passes;
+    return 3 + passes + 1;
 }
 
 template <typename T, typename I>
 int launch_select(const int64_t *n_selected_dev, int64_t n_selected_host, const T *dist,
                   const T *threshold, I *selected, I *n_gt, I *n_eq, int64_t n, void *scratch,
-                  cudaStream_t s, const LoopState *guard) {
-    SelLayout L = sel_layout(scratch);
+                  int64_t max_selected, cudaStream_t s, const LoopState *guard) {
+    SelLayout L = sel_layout(scratch, max_selected);
     const int64_t *gate = n_selected_dev;
     select_count_kernel<T><<<kSelGrid, kSelBlock, 0, s>>>(dist, threshold, n, L, gate, guard);
     KMC_TRY(check_launch("select_count"));
@@ -409,8 +492,20 @@ int launch_select(const int64_t *n_selected_dev, int64_t n_selected_host, const 
     KMC_TRY(check_launch("select_scan"));
     select_write_kernel<T, I><<<kSelGrid, kSelBlock, 0, s>>>(dist, threshold, n, L, selected);
     KMC_TRY(check_launch("select_write"));
-    select_rank_kernel<T, I><<<64, 256, 0, s>>>(dist, L, selected);
-    return check_launch("select_rank");
+    if (max_selected <= kRankAllPairs) {
+        select_rank_kernel<T, I><<<64, 256, 0, s>>>(dist, L, selected);
+        return check_launch("select_rank");
+    }
+    // at most max_selected - 1 entries: ceil(log2(max_selected)) passes cover them
+    const unsigned grid =
+        (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(max_selected, 256),
+                                                         (int64_t)num_sms() * 8));
+    for (int pass = 0; (int64_t(1) << pass) < max_selected; ++pass) {
+        select_merge_kernel<T><<<grid, 256, 0, s>>>(dist, L, pass);
+        KMC_TRY(check_launch("select_merge"));
+    }
+    select_place_kernel<T, I><<<grid, 256, 0, s>>>(L, selected);
+    return check_launch("select_place");
 }
 
 template <typename T, typename I>
@@ -440,7 +535,8 @@ template int launch_threshold<double>(const double *, int64_t, const int64_t *, 
                                       double *, void *, cudaStream_t, const LoopState *);
 #define KMC_INST_RELOC(T, I)                                                                  \
     template int launch_select<T, I>(const int64_t *, int64_t, const T *, const T *, I *, I *, \
-                                     I *, int64_t, void *, cudaStream_t, const LoopState *);  \
+                                     I *, int64_t, void *, int64_t, cudaStream_t,             \
+                                     const LoopState *);                                      \
     template int launch_relocate<T, I>(const int64_t *, int64_t, const T *, const T *,        \
                                        const I *, const I *, const I *, const I *, T *, T *,  \
                                        T *, int64_t, int64_t, int64_t, cudaStream_t,          \

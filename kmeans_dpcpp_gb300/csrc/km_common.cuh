@@ -4,6 +4,7 @@
 // src/*.hpp of kmeans_dpcpp; the per-kernel files cite the exact lines.
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cmath>
@@ -77,6 +78,19 @@ int trim_pools();
 // kmc_trim_cached_memory() hands the unused part back.
 cudaMemPool_t scratch_pool();
 
+// Allocations left before an injected out-of-memory failure (< 0: none);
+// set by kmc_debug_fail_allocation.
+extern std::atomic<long long> g_fail_alloc_after;
+
+// True when the injected failure fires for this allocation (once).
+inline bool injected_alloc_failure() {
+    long long v = g_fail_alloc_after.load();
+    while (v >= 0) {
+        if (g_fail_alloc_after.compare_exchange_weak(v, v - 1)) return v == 0;
+    }
+    return false;
+}
+
 // Stream-ordered scratch allocation (the library's pool, on the caller's stream).
 struct Scratch {
     void *ptr = nullptr;
@@ -89,6 +103,11 @@ struct Scratch {
         ptr = nullptr;
         stream = s;
         if (bytes == 0) bytes = 16;
+        if (injected_alloc_failure()) {
+            set_error("stream-ordered allocation of %zu bytes failed: injected out-of-memory "
+                      "failure (kmc_debug_fail_allocation)", bytes);
+            return KMC_ERR_OUT_OF_MEMORY;
+        }
         cudaMemPool_t pool = scratch_pool();
         cudaError_t e = pool != nullptr ? cudaMallocFromPoolAsync(&ptr, bytes, pool, s)
                                         : cudaMallocAsync(&ptr, bytes, s);

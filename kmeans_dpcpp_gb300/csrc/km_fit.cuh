@@ -63,6 +63,15 @@ struct FitBase {
     // inertia total land in *state_out and *inertia_out (pinned host memory)
     // once the fit's stream reaches this point.
     virtual int finalize_enqueue(LoopState *state_out, double *inertia_out) = 0;
+    // Limit (SM clocks) of the device-side waits of the tensor-core kernels;
+    // with `stall`, the next assignment pass first waits on a barrier that
+    // nothing completes, so that wait runs out (test of the timeout path).
+    // The plain form has no device-side waits and ignores both.
+    virtual int set_wait_limit(long long clocks, int stall) {
+        (void)clocks;
+        (void)stall;
+        return KMC_OK;
+    }
     // Samples re-evaluated in exact arithmetic (mixed form): last pass and total.
     virtual int counters(int64_t *last, int64_t *total, int *device_error) {
         if (last) *last = 0;

@@ -22,6 +22,16 @@ struct LoopState {
     unsigned int pad;
 };
 
+// A kernel of the fit gave up a device-side wait (it then stopped the loop).
+inline int check_device_error(const LoopState &s) {
+    if (s.err != 0) {
+        set_error("a tensor-core kernel of this fit gave up a device-side wait after its time "
+                  "limit; the loop was stopped and its results are not valid");
+        return KMC_ERR_DEVICE_TIMEOUT;
+    }
+    return KMC_OK;
+}
+
 // Lexicographic (value, index) minimum of each of the TM sample rows a thread
 // holds over the 16 threads (lanes differing in bits 0-3, tx = lane & 15) that
 // hold the same rows -- the first minimum of a sequential strict-< scan over
@@ -134,10 +144,14 @@ int launch_threshold(const T *data, int64_t n, const int64_t *topk_dev, int64_t 
                      const LoopState *guard = nullptr);
 // Scratch for launch_select; max_selected bounds n_selected.
 size_t select_scratch_bytes(int64_t max_selected);
+// Kernels launch_select enqueues for a given max_selected.
+int64_t select_launches(int64_t max_selected);
+// `scratch` holds select_scratch_bytes(max_selected) bytes; n_selected (on the
+// device or the host) is at most max_selected.
 template <typename T, typename I>
 int launch_select(const int64_t *n_selected_dev, int64_t n_selected_host, const T *dist,
                   const T *threshold, I *selected, I *n_gt, I *n_eq, int64_t n, void *scratch,
-                  cudaStream_t s, const LoopState *guard = nullptr);
+                  int64_t max_selected, cudaStream_t s, const LoopState *guard = nullptr);
 template <typename T, typename I>
 int launch_relocate(const int64_t *n_empty_dev, int64_t n_empty_host, const T *X, const T *w,
                     const I *labels, const I *selected, const I *n_gt, const I *empty_list,

@@ -58,13 +58,32 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 }
 
 // Waits for the phase with the given parity.  Returns false (and raises the
-// CTA error flag) on timeout, or when another role already raised it.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *err) {
+// CTA error flag) after `limit` SM clocks, or as soon as another role has
+// raised the flag.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *err,
+                                          long long limit = kWaitClocks) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (true) {
         if (mbar_try_wait(bar, parity)) return true;
         if (*err) return false;
+        if (clock64() - t0 > limit) {
+            *err = 1;
+            return false;
+        }
+    }
+}
+
+// Wait used while winding down: it ignores the error flag and returns only
+// when the phase completes (true) or after kWaitClocks (false).  It waits for
+// work that was already issued -- bulk copies into this CTA's shared memory,
+// committed tensor-core operations -- which always completes, so a CTA never
+// frees TMEM or exits with such work still writing.
+__device__ __forceinline__ bool mbar_wait_drain(uint64_t *bar, uint32_t parity, volatile int *err) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (true) {
+        if (mbar_try_wait(bar, parity)) return true;
         if (clock64() - t0 > kWaitClocks) {
             *err = 1;
             return false;

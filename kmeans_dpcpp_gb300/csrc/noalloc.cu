@@ -15,7 +15,10 @@
 // calls whose kernels overlap (different streams, or different host threads)
 // race on it.  The first call on a device looks up the array's address with
 // cudaGetSymbolAddress (which may load this module onto the device); make
-// that first call before capturing a stream into a graph.
+// that first call before capturing a stream into a graph.  The address is
+// kept together with the unique id of the context it belongs to: after a
+// device reset (a new primary context, the module loaded again) the next call
+// looks the address up again instead of using the old one.
 #include <mutex>
 
 #include "km_kernels.cuh"
@@ -31,20 +34,60 @@ static __device__ __align__(256) unsigned char g_select_scratch[kNoAllocScratchB
 
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
-void *g_scratch_ptr[kMaxDevices] = {};
+struct ScratchAddr {
+    unsigned long long ctx_id;  // context the address belongs to
+    void *ptr;
+};
+ScratchAddr g_scratch[kMaxDevices] = {};
 
-// Address of this device's scratch array; the device must be current.
+// Unique id (over the life of the process) of the calling thread's current
+// context, through the driver entry points the runtime exposes; 0 if unknown.
+unsigned long long current_context_id() {
+    using GetCurrentFn = int (*)(void **);
+    using GetIdFn = int (*)(void *, unsigned long long *);
+    static GetCurrentFn get_current = nullptr;
+    static GetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetIdFn>(f);
+        (void)cudaGetLastError();
+    });
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current == nullptr || get_id == nullptr || get_current(&ctx) != 0 || ctx == nullptr ||
+        get_id(ctx, &id) != 0)
+        return 0;
+    return id;
+}
+
+// Address of this device's scratch array; the device must be current.  It is
+// looked up once per device and context.
 int scratch_for_current_device(void **out) {
     int dev = -1;
     KMC_CUDA_TRY(cudaGetDevice(&dev));
     KMC_CHECK_ARG(dev >= 0 && dev < kMaxDevices, "device ordinal %d is out of range", dev);
+    // 0 when no context is current on this thread yet: the lookup below then
+    // makes the device's primary context current
+    const unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (g_scratch_ptr[dev] == nullptr) {
+    ScratchAddr &a = g_scratch[dev];
+    if (a.ptr == nullptr || ctx == 0 || a.ctx_id != ctx) {
         void *p = nullptr;
         KMC_CUDA_TRY(cudaGetSymbolAddress(&p, g_select_scratch));
-        g_scratch_ptr[dev] = p;
+        a.ptr = p;
+        a.ctx_id = current_context_id();
     }
-    *out = g_scratch_ptr[dev];
+    *out = a.ptr;
     return KMC_OK;
 }
 
@@ -72,6 +115,6 @@ extern "C" int kmc_select_samples_far_from_centroid_noalloc_f32_i32(
     KMC_TRY(scratch_for_current_device(&scratch));
     return launch_select<float, int32_t>(nullptr, n_selected, distance_to_centroid, threshold,
                                          selected_samples_idx, n_selected_gt_threshold,
-                                         n_selected_eq_threshold, n_samples, scratch,
+                                         n_selected_eq_threshold, n_samples, scratch, n_selected,
                                          reinterpret_cast<cudaStream_t>(stream));
 }

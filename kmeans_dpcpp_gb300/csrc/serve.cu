@@ -367,7 +367,8 @@ struct BatchEngine {
         KMC_TRY(launch_fill<int32_t>(counters, 0, 1, s));
         KMC_TRY(launch_fill<int32_t>(counters + 1, 1, 1, s));
         KMC_TRY(launch_select<float, int32_t>(nullptr, m, sm.sq_dist, sm.thr, sm.selected,
-                                              counters, counters + 1, h.n, sm.sel_scratch, s));
+                                              counters, counters + 1, h.n, sm.sel_scratch, h.k,
+                                              s));
         KMC_TRY(launch_relocate<float, int32_t>(nullptr, m, h.X, h.w, h.labels, sm.selected,
                                                 counters, sm.empty_list, sm.Cn, sm.sizes,
                                                 sm.sq_dist, h.n, h.d, h.k, s));
@@ -819,8 +820,9 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
                 }
                 const volatile LoopState *hs = a.hstate;
                 if (a.final_enqueued) {
+                    // a tensor-core kernel that gave up a wait marks the request failed
                     KMC_TRY(finish(a, (int64_t)hs->n_iter, *(const volatile double *)a.hinertia,
-                                   KMC_OK));
+                                   hs->err != 0 ? KMC_ERR_DEVICE_TIMEOUT : KMC_OK));
                     a.fit.reset();
                     active.erase(active.begin() + (int64_t)t);
                     progressed = true;

@@ -282,43 +282,59 @@ void accumulate(const T *X, const T *w, const I *labels, T *sums, T *sizes, int6
     for (int64_t j = 0; j < k; ++j) sizes[j] = (T)sz[j];
 }
 
+// One pass of the loop body of src/kmeans_lloyd_driver.hpp:86-353 from the
+// centroids `cur`: labels against cur (fused step, :86-143), sums, sizes and
+// the empty list (:155-170), relocation when a cluster is empty (:217-312),
+// division and the centroid shifts (:317-341) into `newc`.  Returns the
+// float64 total of the shifts cast to T (:343-348); *relocated is set when the
+// pass relocated.
+template <typename T, typename I>
+T iteration(const T *X, const T *w, const T *cur, I *labels, T *newc, int64_t n, int64_t d,
+            int64_t k, bool *relocated) {
+    std::vector<T> hn(k), sizes(k), sh(k);
+    std::vector<I> list(k);
+    half_norm<T>(cur, hn.data(), d, k);
+    assignment<T, I>(X, cur, hn.data(), labels, n, d, k);
+    accumulate<T, I>(X, w, labels, newc, sizes.data(), n, d, k);
+    I n_empty = 0;
+    for (int64_t j = 0; j < k; ++j)
+        if (sizes[j] == T(0)) list[n_empty++] = (I)j;
+    *relocated = n_empty > 0;
+    if (n_empty > 0) {
+        std::vector<T> sq(n);
+        inertia<T, I>(X, nullptr, cur, labels, sq.data(), n, d, k);
+        relocate<T, I>((int64_t)n_empty, X, w, labels, list.data(), sq.data(), newc, sizes.data(),
+                       sq.data(), n, d, k);
+    }
+    for (int64_t j = 0; j < k; ++j) {
+        T acc = T(0);
+        for (int64_t f = 0; f < d; ++f) {
+            T c = newc[f * k + j] / sizes[j];
+            newc[f * k + j] = c;
+            T diff = cur[f * k + j] - c;
+            acc = fma_t(diff, diff, acc);
+        }
+        sh[j] = acc;
+    }
+    long double tot = 0.0L;
+    for (int64_t j = 0; j < k; ++j) tot += (long double)sh[j];
+    return (T)(double)tot;
+}
+
 // src/kmeans_lloyd_driver.hpp:21-431
 template <typename T, typename I>
 int64_t driver(const T *X, const T *w, T *init_c, I *labels, T *res_c, int64_t n, int64_t d,
                int64_t k, double tol, int64_t max_iter, double *inertia_out,
                int64_t *relocations_out) {
-    std::vector<T> hn(k), sizes(k), sh(k), sq(n), newc(d * k);
-    std::vector<I> list(k);
+    std::vector<T> hn(k), sq(n), newc(d * k);
     const T tol_t = (T)tol;
     T shift_t = std::numeric_limits<T>::infinity();
     int64_t it = 0, relocations = 0;
     T *cur = init_c;
     while (it < max_iter && shift_t > tol_t) {
-        half_norm<T>(cur, hn.data(), d, k);
-        assignment<T, I>(X, cur, hn.data(), labels, n, d, k);
-        accumulate<T, I>(X, w, labels, newc.data(), sizes.data(), n, d, k);
-        I n_empty = 0;
-        for (int64_t j = 0; j < k; ++j)
-            if (sizes[j] == T(0)) list[n_empty++] = (I)j;
-        if (n_empty > 0) {
-            ++relocations;
-            inertia<T, I>(X, nullptr, cur, labels, sq.data(), n, d, k);
-            relocate<T, I>((int64_t)n_empty, X, w, labels, list.data(), sq.data(), newc.data(),
-                           sizes.data(), sq.data(), n, d, k);
-        }
-        for (int64_t j = 0; j < k; ++j) {
-            T acc = T(0);
-            for (int64_t f = 0; f < d; ++f) {
-                T c = newc[f * k + j] / sizes[j];
-                newc[f * k + j] = c;
-                T diff = cur[f * k + j] - c;
-                acc = fma_t(diff, diff, acc);
-            }
-            sh[j] = acc;
-        }
-        long double tot = 0.0L;
-        for (int64_t j = 0; j < k; ++j) tot += (long double)sh[j];
-        shift_t = (T)(double)tot;
+        bool rel = false;
+        shift_t = iteration<T, I>(X, w, cur, labels, newc.data(), n, d, k, &rel);
+        if (rel) ++relocations;
         std::memcpy(cur, newc.data(), sizeof(T) * d * k);
         ++it;
     }
@@ -461,6 +477,13 @@ void kmref_set_num_threads(int t) {
                                 T *sums, T *sizes, int64_t n, int64_t d, int64_t k) {          \
         assignment<T, int64_t>(X, C, hn, lab, n, d, k);                                       \
         accumulate<T, int64_t>(X, w, lab, sums, sizes, n, d, k);                               \
+    }                                                                                         \
+    double kmref_iteration_##SUF(const T *X, const T *w, const T *cur, int64_t *lab, T *nxt,   \
+                                 int64_t n, int64_t d, int64_t k, int64_t *relocated) {        \
+        bool rel = false;                                                                     \
+        const T sh = iteration<T, int64_t>(X, w, cur, lab, nxt, n, d, k, &rel);               \
+        *relocated = rel ? 1 : 0;                                                             \
+        return (double)sh;                                                                    \
     }                                                                                         \
     int64_t kmref_driver_##SUF(const T *X, const T *w, T *ic, int64_t *lab, T *rc, int64_t n,  \
                                int64_t d, int64_t k, double tol, int64_t max_iter,            \

@@ -52,6 +52,9 @@ def lib():
             getattr(L, f"kmref_assignment_{suf}").argtypes = [_p] * 4 + [_c_i64] * 3
             getattr(L, f"kmref_inertia_{suf}").argtypes = [_p] * 5 + [_c_i64] * 3
             getattr(L, f"kmref_fused_step_{suf}").argtypes = [_p] * 7 + [_c_i64] * 3
+            f = getattr(L, f"kmref_iteration_{suf}")
+            f.argtypes = [_p] * 5 + [_c_i64] * 3 + [_p]
+            f.restype = _c_dbl
             f = getattr(L, f"kmref_driver_{suf}")
             f.argtypes = [_p] * 5 + [_c_i64] * 3 + [_c_dbl, _c_i64, _p, _p]
             f.restype = _c_i64
@@ -202,6 +205,21 @@ def fused_lloyd_single_step(X_t, w, C, hn=None):
     getattr(lib(), f"kmref_fused_step_{_suf(X_t.dtype)}")(_ptr(X_t), _ptr(w), _ptr(C), _ptr(hn), _ptr(lab),
                                                           _ptr(sums), _ptr(sizes), n, d, k)
     return lab, sums, sizes
+
+
+def lloyd_iteration(X_t, w, C):
+    """One pass of the driver's loop body from centroids C (d, k).
+
+    Returns (labels against C, next centroids (d, k), shift total, relocated)."""
+    X_t, w, C = _c(X_t), _c(w), _c(C)
+    d, n = X_t.shape
+    k = C.shape[1]
+    lab = np.empty(n, np.int64)
+    nxt = np.empty_like(C)
+    rel = np.zeros(1, np.int64)
+    sh = getattr(lib(), f"kmref_iteration_{_suf(X_t.dtype)}")(
+        _ptr(X_t), _ptr(w), _ptr(C), _ptr(lab), _ptr(nxt), n, d, k, _ptr(rel))
+    return lab, nxt, float(sh), bool(rel[0])
 
 
 def kmeans_lloyd_driver(X_t, w, init_C, tol, max_iter):

@@ -148,3 +148,27 @@ def test_oracle_relocation_multiple_empty(oracle):
         assert sz2[cl] == 1.0
         assert inr2[order[r]] == 0.0
     assert sz2.sum() == n
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_oracle_iteration_chains_to_the_driver(oracle, dt):
+    """lloyd_iteration is the driver's loop body: chained from the same start (one centroid
+    forced empty, so the first pass relocates) it reaches the driver's centroids bit for bit,
+    and its last labels are the assignment against its last input centroids."""
+    import bench
+
+    X, _, _ = bench.make_blobs(3000, 4, 6, (-10, 10), 1.0, 21, dtype=dt)
+    C0 = bench.random_row_init(X, 6, 21, far_first=True)
+    w = np.ones(X.shape[1], dt)
+    it, _, C_drv, _, rel = oracle.kmeans_lloyd_driver(X, w, C0, 0.0, 4)
+    assert it == 4 and rel >= 1
+    C = C0.copy()
+    relocated = []
+    for _ in range(4):
+        lab, C_next, shift, r = oracle.lloyd_iteration(X, w, C)
+        np.testing.assert_array_equal(lab, oracle.assignment(X, C))
+        relocated.append(r)
+        C = C_next
+    assert relocated[0]
+    np.testing.assert_array_equal(C, C_drv)
+    assert shift >= 0.0

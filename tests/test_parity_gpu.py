@@ -117,7 +117,7 @@ def test_distances_and_inertia_bit_exact(kdp, oracle, n, d, k, dt):
 
 
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
-@pytest.mark.parametrize("topk", [1, 2, 3, 17, 1000])
+@pytest.mark.parametrize("topk", [1, 2, 3, 17, 1000, 4096, 4097, 100000])
 @pytest.mark.parametrize("ties", [False, True])
 def test_threshold_and_select_parity(kdp, oracle, dt, topk, ties):
     import torch
@@ -138,6 +138,37 @@ def test_threshold_and_select_parity(kdp, oracle, dt, topk, ties):
     sel_o, ng_o, nq_o = oracle.select_samples_far_from_centroid(topk, x, thr_o, fill=-5)
     assert (H(ngt).item(), H(neq).item()) == (ng_o, nq_o)
     np.testing.assert_array_equal(H(sel), sel_o)
+
+
+def test_select_many_samples_is_fast_and_exact(kdp, oracle):
+    """300,000 selections out of 2M samples: the strictly-greater samples are ranked by a
+    merge sort (O(m log^2 m)), not by counting all pairs (~10^11 compares here)."""
+    import time
+
+    import torch
+
+    rng = np.random.default_rng(12)
+    x = np.round(rng.standard_gamma(4, size=2_000_000), 2).astype(np.float32)
+    topk = 300_000
+    thr_o = oracle.compute_threshold(x, topk)
+    xg, thr = T(x), T(np.array(thr_o, np.float32))
+    sel = T(np.full(x.size, -5), np.int32)
+    ngt, neq = T(np.zeros(()), np.int32), T(np.ones(()), np.int32)
+    kdp.select_samples_far_from_centroid(topk, xg, thr, sel, ngt, neq, 256, None)[0].wait()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        sel.fill_(-5)
+        ngt.fill_(0)
+        neq.fill_(1)
+        kdp.select_samples_far_from_centroid(topk, xg, thr, sel, ngt, neq, 256, None)[0].wait()
+    torch.cuda.synchronize()
+    per_call = (time.perf_counter() - t0) / 3
+    sel_o, ng_o, nq_o = oracle.select_samples_far_from_centroid(topk, x, thr_o, fill=-5)
+    assert (H(ngt).item(), H(neq).item()) == (ng_o, nq_o)
+    assert ng_o > 4096                           # the merge-sort path ran
+    np.testing.assert_array_equal(H(sel), sel_o)
+    assert per_call < 0.25, per_call
 
 
 @pytest.mark.parametrize("n_empty", [1, 2, 3, 5])
