@@ -73,7 +73,13 @@ WORKLOADS = {
                far_first=True, desc="5M x 14 float32 Gaussian blobs, k=127, centroid 0 = 1e3*ones"),
     "c1": dict(n=50_000, d=14, centers=16, k=16, box=(-10.0, 10.0), std=1.0, seed=0,
                far_first=False, desc="50k x 14 float32 Gaussian blobs, k=16"),
+    "c2f64": dict(n=5_000_000, d=14, centers=127, k=127, box=(-10.0, 10.0), std=1.5, seed=1,
+                  far_first=True, dtype="f64",
+                  desc="5M x 14 float64 Gaussian blobs, k=127, centroid 0 = 1e3*ones"),
 }
+
+# Nominal dense FP64 rate of one GB300 (no measured FP64 peak is available).
+FP64_NOMINAL_TFLOPS = 1.25
 
 FORMS = {"plain": 0, "mixed-bf16": 1, "mixed-fp16": 2}
 
@@ -134,7 +140,8 @@ def workload(name, n=None):
 
 def workload_data(name, n=None):
     w = workload(name, n)
-    X_t, _, _ = make_blobs(w["n"], w["d"], w["centers"], w["box"], w["std"], w["seed"])
+    dt = np.float64 if w.get("dtype") == "f64" else np.float32
+    X_t, _, _ = make_blobs(w["n"], w["d"], w["centers"], w["box"], w["std"], w["seed"], dtype=dt)
     C0 = random_row_init(X_t, w["k"], w["seed"], far_first=w["far_first"])
     return X_t, C0
 
@@ -298,7 +305,8 @@ def run_reference(args, world, rank):
     line = {
         "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if X_t.dtype == np.float64 else "f32",
         "data": "synthetic", "impl": "reference",
         "config": {"workload": args.workload, "desc": w["desc"], "n": w["n"], "d": w["d"], "k": w["k"]},
         "cpu_baseline": {"value": value, "unit": "iter/s", "cores": kmref.num_threads(),
@@ -320,9 +328,10 @@ def _time_form(L, capi, Xg, wg, C0, n, d, k, form, steps, warmup, world, local, 
     fit = ctypes.c_void_p()
     c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     c0.record(stream)
-    capi.check(L.kmc_fit_create_f32_i32(Xg.data_ptr(), wg.data_ptr(), cur.data_ptr(), lab.data_ptr(),
-                                        res_c.data_ptr(), n, d, k, 0.0, warmup + steps + 1,
-                                        FORMS[form], stream.cuda_stream, ctypes.byref(fit)))
+    create = L.kmc_fit_create_f64_i32 if Xg.dtype == torch.float64 else L.kmc_fit_create_f32_i32
+    capi.check(create(Xg.data_ptr(), wg.data_ptr(), cur.data_ptr(), lab.data_ptr(),
+                      res_c.data_ptr(), n, d, k, 0.0, warmup + steps + 1,
+                      FORMS[form], stream.cuda_stream, ctypes.byref(fit)))
     c1.record(stream)
     c1.synchronize()
     prep_ms = c0.elapsed_time(c1)
@@ -373,11 +382,16 @@ def _time_form(L, capi, Xg, wg, C0, n, d, k, form, steps, warmup, world, local, 
             "clocks": clk.summary() if sample_clocks else None}
 
 
-def _roofline(workload, form, n, d, k, kern_ms, clocks, sm_count):
+def _roofline(workload, form, n, d, k, kern_ms, clocks, sm_count, f64=False):
     peaks, peak_src = measured_peaks()
     flops = 2.0 * n * k * d
     achieved = flops / (kern_ms * 1e-3) / 1e12
-    if form == "plain":
+    if f64:
+        r = {"bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+             "peak_source": "nominal dense FP64 rate of a GB300 (no measured FP64 peak); the "
+                            "plain float64 form runs on the FP64 pipe",
+             "kernel": "tile_kernel (exact fused assignment + accumulation, float64)"}
+    elif form == "plain":
         clk_mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
         peak = sm_count * 128 * 2 * clk_mhz * 1e6 / 1e12
         r = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -399,7 +413,7 @@ def _roofline(workload, form, n, d, k, kern_ms, clocks, sm_count):
               "flops_per_launch": flops,
               # plain: X (fp32) once + labels; mixed: the fp16/bf16 image for the
               # contraction, the fp32 rows for the exact sums, labels
-              "algorithmic_bytes_per_launch": n * d * (4 if form == "plain" else 6) + 4 * n})
+              "algorithmic_bytes_per_launch": n * d * ((8 if f64 else 4) if form == "plain" else 6) + 4 * n})
     return r
 
 
@@ -634,26 +648,29 @@ def run_gb300(args, world, rank, local):
     w = workload(args.workload, args.n)
     n, d, k = w["n"], w["d"], w["k"]
     X_t, C0 = workload_data(args.workload, args.n)
-    form = "mixed-fp16" if args.form == "auto" else args.form
+    f64 = X_t.dtype == np.float64
+    # the mixed tensor-core forms take float32 data
+    form = ("plain" if f64 else "mixed-fp16") if args.form == "auto" else args.form
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
 
     Xg = torch.from_numpy(X_t).cuda()
-    wg = torch.ones(n, dtype=torch.float32, device="cuda")
+    wg = torch.ones(n, dtype=Xg.dtype, device="cuda")
     head = _time_form(L, capi, Xg, wg, C0, n, d, k, form, args.steps, args.warmup, world, local, True)
     forms = {form: head}
-    if not args.no_compare:
+    if not args.no_compare and not f64:
         for other in ("plain", "mixed-bf16", "mixed-fp16"):
             if other not in forms:
                 st = min(args.steps, 10) if other == "plain" else args.steps
                 forms[other] = _time_form(L, capi, Xg, wg, C0, n, d, k, other, st, args.warmup, world,
                                           local, False)
-    roofline = _roofline(args.workload, form, n, d, k, head["kernel_ms"], head["clocks"], sm_count)
+    roofline = _roofline(args.workload, form, n, d, k, head["kernel_ms"], head["clocks"], sm_count,
+                         f64=f64)
 
     # ---- end to end through the drop-in surface, host buffers ----
     e2e = None
     if not args.no_e2e:
         X_h = torch.from_numpy(X_t).pin_memory()
-        w_h = torch.ones(n, dtype=torch.float32).pin_memory()
+        w_h = torch.ones(n, dtype=Xg.dtype).pin_memory()
         C_h = torch.from_numpy(C0.copy()).pin_memory()
         lab_h = torch.empty(n, dtype=torch.int32).pin_memory()
         Cres_h = torch.empty_like(C_h).pin_memory()
@@ -676,8 +693,8 @@ def run_gb300(args, world, rank, local):
         torch.cuda.synchronize()
         t_e2e = all_max(world, time.perf_counter() - t0)
         assert n_iter == args.steps
-        h2d = X_t.nbytes + 4 * n + C0.nbytes
-        d2h = 4 * n + C0.nbytes + 4
+        h2d = X_t.nbytes + X_t.itemsize * n + C0.nbytes
+        d2h = 4 * n + C0.nbytes + X_t.itemsize
         e2e = {"value": world * n_iter / t_e2e, "unit": "iter/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h,
                "note": "one kmeans_lloyd_driver call (form=%s) of K iterations (tol=0): pinned-host "
@@ -689,7 +706,7 @@ def run_gb300(args, world, rank, local):
         "metric": METRIC, "value": head["value"], "unit": "iter/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32" if form == "plain" else form.split("-")[1],
+        "dtype": ("f64" if f64 else "f32") if form == "plain" else form.split("-")[1],
         "data": "synthetic",
         "config": {"workload": args.workload, "desc": w["desc"], "n": n, "d": d, "k": k,
                    "form": form, "parallelism": f"replicas{world}",

@@ -39,6 +39,7 @@ typedef struct CUevent_st *kmc_event_t;   /* ABI-identical to cudaEvent_t  */
 #define KMC_ERR_OUT_OF_MEMORY 3
 #define KMC_ERR_UNSUPPORTED 4
 #define KMC_ERR_DEVICE_TIMEOUT 5
+#define KMC_ERR_CANCELLED 6
 
 /* Message describing the last failure on the calling thread. */
 const char *kmc_last_error(void);
@@ -615,6 +616,77 @@ typedef struct {
     int32_t status;      /* KMC_OK or an error code */
     int32_t pad;
 } kmc_serve_result_t;
+/* ---- request server ------------------------------------------------------------------
+ * No counterpart in the reference.  Each request is what the reference does per
+ * call, on the caller's device buffers: a fit is kmeans_lloyd_driver
+ * (_kmeans_lloyd.cpp:1427-1448 -> src/kmeans_lloyd_driver.hpp:21-431, without
+ * overwriting the initial centroids), a prediction is assignment
+ * (_kmeans_lloyd.cpp:1369-1380) against a fitted model, a transform is
+ * compute_centroid_to_sample_distances (_kmeans_lloyd.cpp:1354-1367).
+ *
+ * kmc_server_open starts a server of one form (KMC_FORM_*) with an HBM budget for
+ * the memory it allocates and a limit on running requests.  Submissions return
+ * a ticket at once; requests are admitted in submission order while the running
+ * count and the budget allow (a prediction waits, without blocking the queue,
+ * for the fit whose model it names).  The inputs must have been written on the
+ * stream given to kmc_server_open (or be complete before the submission) and
+ * stay unchanged until the ticket finishes; the outputs are complete when the
+ * ticket reports KMC_REQ_DONE.  A fit's final centroids stay on the device as
+ * its model (predictions and transforms name the fit's ticket) until
+ * kmc_server_release or kmc_server_close.  The plain form advances all running
+ * requests together in the batched engine (bit-equal to single plain fits); the
+ * mixed forms run one tensor-core session per request on a pool of streams.
+ * A server is driven by its callers: submissions only queue, and
+ * kmc_server_poll / kmc_server_wait admit requests and make progress (in the
+ * plain form each such step runs one engine iteration of every running
+ * request; in the mixed forms it launches work and returns).  Calls on one
+ * server must not overlap (one host thread at a time).  A request's own failure is its status (KMC_ERR_OUT_OF_MEMORY when it
+ * can never fit the budget, KMC_ERR_CANCELLED, KMC_ERR_DEVICE_TIMEOUT, ...); the
+ * functions' return codes report invalid calls and CUDA errors. */
+typedef struct kmc_server_s *kmc_server_t;
+#define KMC_REQ_PENDING 0
+#define KMC_REQ_RUNNING 1
+#define KMC_REQ_DONE 2
+#define KMC_REQ_FAILED 3
+#define KMC_REQ_CANCELLED 4
+int kmc_server_open(int form, int64_t hbm_budget_bytes, int64_t max_active, kmc_stream_t stream,
+                    kmc_server_t *server_out);
+/* X_t (d, n), sample_weight (n), init_centroids_t (d, k) are read; labels_out (n)
+ * and centroids_out (d, k) are written. */
+int kmc_server_submit_fit_f32(kmc_server_t server, const float *X_t, const float *sample_weight,
+                              const float *init_centroids_t, int32_t *labels_out,
+                              float *centroids_out, int64_t n_samples, int64_t n_features,
+                              int64_t n_clusters, double tol, int64_t max_iter,
+                              int64_t *ticket_out);
+/* Labels of X_t (d, n) against the model of fit ticket model_ticket (d and k are
+ * the model's).  The plain form reports inertia 0; the mixed forms report the
+ * unit-weight inertia of the labels. */
+int kmc_server_submit_predict_f32(kmc_server_t server, const float *X_t, int64_t model_ticket,
+                                  int32_t *labels_out, int64_t n_samples, int64_t *ticket_out);
+/* distances_out (k, n) = Euclidean distances to the model's centroids;
+ * the result's inertia is their float64 sum. */
+int kmc_server_submit_transform_f32(kmc_server_t server, const float *X_t, int64_t model_ticket,
+                                    float *distances_out, int64_t n_samples,
+                                    int64_t *ticket_out);
+/* Makes one step of progress, then reports the ticket's state
+ * (KMC_REQ_*) and, once it finished, its status, iterations and inertia. */
+int kmc_server_poll(kmc_server_t server, int64_t ticket, int *state_out, int *status_out,
+                    int64_t *n_iter_out, double *inertia_out);
+/* Drives the server until the ticket finished. */
+int kmc_server_wait(kmc_server_t server, int64_t ticket, int *status_out, int64_t *n_iter_out,
+                    double *inertia_out);
+/* A pending request is dropped; a running one stops after the work it has in
+ * flight.  Either ends with status KMC_ERR_CANCELLED (its outputs are then
+ * undefined); predictions waiting for a cancelled fit fail.  No effect on a
+ * finished ticket. */
+int kmc_server_cancel(kmc_server_t server, int64_t ticket);
+/* Frees a finished ticket's record and, for a fit, its model. */
+int kmc_server_release(kmc_server_t server, int64_t ticket);
+int kmc_server_stats(kmc_server_t server, int64_t *pending_out, int64_t *running_out,
+                     int64_t *bytes_in_use_out);
+/* Cancels what has not finished, waits for the work in flight, frees everything. */
+int kmc_server_close(kmc_server_t server);
+
 int kmc_serve_bytes_needed(int32_t kind, int64_t n_samples, int64_t n_features,
                            int64_t n_clusters, int form, int64_t *bytes_out);
 int kmc_serve_run(const kmc_serve_request_t *requests, int64_t n_requests, int form,

@@ -73,7 +73,8 @@ def parse_header(path: str = HEADER):
 
 def _ctype(t: str):
     t = t.replace("const ", "").strip()
-    if t.endswith("*") or t in ("kmc_stream_t", "kmc_event_t", "kmc_fit_t", "kmc_batch_t"):
+    if t.endswith("*") or t in ("kmc_stream_t", "kmc_event_t", "kmc_fit_t", "kmc_batch_t",
+                                "kmc_server_t"):
         if t == "char *" or t == "char*":
             return ctypes.c_char_p
         return ctypes.c_void_p

@@ -218,6 +218,36 @@ __device__ __forceinline__ void mask_tail(uint32_t (&r)[32], int64_t j0, int64_t
     }
 }
 
+// The test v >= thr as a fused multiply-add with saturation, which runs on
+// the FMA pipe instead of the ALU pipe the compares and selects use.  thrp is
+// the float just below thr and K = 2 / ulp(thrp), a power of two: for every
+// float v > thrp (equivalently v >= thr), v - thrp >= ulp(thrp) / 2 (v lies
+// in thrp's binade or above, or at most one binade below it, where floats are
+// spaced ulp(thrp) / 2), so the exact K (v - thrp) is >= 1 and saturates to
+// exactly 1; for v <= thrp it is <= 0 and saturates to 0 (a NaN score also
+// gives 0, as a NaN compare is false).  thrp K is exact.  Products that
+// overflow give +-inf, which saturate to the right side as well.  Thresholds
+// whose neighbour's exponent is too small for K to be finite (|thr| below
+// about 2^-88), zero, infinite or NaN thresholds take the compare path.
+struct HotTest {
+    float K, nK;
+    bool ok;
+    __device__ __forceinline__ float hot(float v) const { return __saturatef(fmaf(v, K, nK)); }
+};
+
+__device__ __forceinline__ HotTest hot_test(float thr) {
+    HotTest h;
+    const uint32_t b = __float_as_uint(thr);
+    const uint32_t e = (b >> 23) & 0xffu;
+    h.ok = e >= 40u && e < 255u;
+    // the float just below thr (|thr| >= 2^-87 here, so it is normal)
+    const uint32_t pb = (b & 0x80000000u) ? b + 1u : b - 1u;
+    const uint32_t ep = (pb >> 23) & 0xffu;
+    h.K = __uint_as_float(h.ok ? (278u - ep) << 23 : 0x3f800000u);  // 2^(151 - ep)
+    h.nK = -__uint_as_float(pb) * h.K;
+    return h;
+}
+
 // OR over the 64 epilogue threads of TMEM lane quadrant q (the two warps that
 // scan the two column halves of the same rows), named barrier 8 + q.  Only
 // these two warps exchange data, so the other quadrants are not held back.
@@ -514,13 +544,32 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
             const float thr = fmaxf(Mh, Mo) - E2;
             const bool win = (Mh > Mo) || (Mh == Mo && h == 0);
             uint32_t hot1 = 0u, hot2 = 0u;
+            const HotTest ht = hot_test(thr);
+            if (ht.ok) {
+                // the masks on the FMA pipe: 0 / 1 per maximum, summed as
+                // exact powers of two in two 16-bit float halves
+                float l1 = 0.f, l2 = 0.f, h2 = 0.f;
 #pragma unroll
-            for (int t = 0; t < kSub; ++t) {
-                const float m = kP1s ? my_p1[t * 32 * kEpiWarps] : P1[kP1s ? 0 : t];
-                hot1 |= (m >= thr) ? (1u << t) : 0u;
+                for (int t = 0; t < kSub; ++t) {
+                    const float m = kP1s ? my_p1[t * 32 * kEpiWarps] : P1[kP1s ? 0 : t];
+                    l1 = fmaf(ht.hot(m), (float)(1u << t), l1);
+                }
+#pragma unroll
+                for (int t = 0; t < 16; ++t) {
+                    l2 = fmaf(ht.hot(P2[t]), (float)(1u << t), l2);
+                    h2 = fmaf(ht.hot(P2[16 + t]), (float)(1u << t), h2);
+                }
+                hot1 = __float2uint_rz(l1);
+                hot2 = __float2uint_rz(l2) | (__float2uint_rz(h2) << 16);
+            } else {
+#pragma unroll
+                for (int t = 0; t < kSub; ++t) {
+                    const float m = kP1s ? my_p1[t * 32 * kEpiWarps] : P1[kP1s ? 0 : t];
+                    hot1 |= (m >= thr) ? (1u << t) : 0u;
+                }
+#pragma unroll
+                for (int t = 0; t < 32; ++t) hot2 |= (P2[t] >= thr) ? (1u << t) : 0u;
             }
-#pragma unroll
-            for (int t = 0; t < 32; ++t) hot2 |= (P2[t] >= thr) ? (1u << t) : 0u;
             bool loser_hot = fminf(Mh, Mo) >= thr;
             if (!(thr == thr)) {  // cannot happen with finite operands; recheck all
                 hot1 = kAll1;
@@ -1432,6 +1481,8 @@ int make_mixed_fit(const FitParams<T, I> &p, int form, std::unique_ptr<FitBase> 
         return KMC_OK;
     }
 }
+
+bool mixed_fit_supported(int64_t d, int64_t k) { return MixedFit<int32_t>::supported(d, k); }
 
 template int make_mixed_fit<float, int32_t>(const FitParams<float, int32_t> &, int,
                                             std::unique_ptr<FitBase> *);

@@ -131,5 +131,7 @@ struct PlainFit : FitBase {
 // Mixed tensor-core form (kernels_mixed.cu); float32 data only.
 template <typename T, typename I>
 int make_mixed_fit(const FitParams<T, I> &p, int form, std::unique_ptr<FitBase> *out);
+// Whether the mixed form takes n_features = d and n_clusters = k.
+bool mixed_fit_supported(int64_t d, int64_t k);
 
 }  // namespace kmc

@@ -19,6 +19,7 @@
 #include <chrono>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <memory>
 #include <thread>
 #include <vector>
@@ -432,20 +433,29 @@ struct BatchEngine {
 };
 
 // ---------------------------------------------------------------------------
-// Serving loop
+// Serving: a request server over caller buffers (kmc_server_*) and, built on
+// it, the replay harness of a request stream (kmc_serve_run)
 // ---------------------------------------------------------------------------
-namespace {
+namespace serving {
 
-// Device bytes one request holds while admitted (its data, centroids and
-// labels, plus the engine's or the fit session's working memory).
-int64_t request_bytes(int kind, int64_t n, int64_t d, int64_t k, int form) {
-    const int64_t d4 = ceil_div<int64_t>(std::max<int64_t>(d, 1), 4) * 4;
+// Bytes of a request's own data: samples, weights, centroids and labels, and
+// for a transform its (k, n) distances.
+int64_t data_bytes(int kind, int64_t n, int64_t d, int64_t k) {
     int64_t b = (int64_t)(align256(sizeof(float) * n * d) + align256(sizeof(float) * n) +
                           align256(sizeof(float) * d * k) + align256(sizeof(int32_t) * n));
+    if (kind == 2) b += (int64_t)align256(sizeof(float) * n * k);
+    return b;
+}
+
+// Device bytes the server allocates for a request while it runs: a fit's
+// model (its working centroids, kept after the fit for predictions), a
+// transform's checksum scratch, and the batched engine's slot or the
+// tensor-core session's working memory.
+int64_t work_bytes(int kind, int64_t n, int64_t d, int64_t k, int form) {
+    const int64_t d4 = ceil_div<int64_t>(std::max<int64_t>(d, 1), 4) * 4;
+    int64_t b = (int64_t)align256(sizeof(float) * d * k);
     if (kind == 2) {
-        // distances, their float64 checksum, and the engine's assignment-sized slot
-        b += (int64_t)(align256(sizeof(float) * n * k) +
-                       align256(sizeof(double) * (sum_partials_size() + 1)) +
+        b += (int64_t)(align256(sizeof(double) * (sum_partials_size() + 1)) +
                        slot_bytes(B_ASSIGN, n, d, k));
     } else if (form == KMC_FORM_PLAIN) {
         b += (int64_t)slot_bytes(kind == 0 ? B_FIT : B_ASSIGN, n, d, k);
@@ -458,54 +468,47 @@ int64_t request_bytes(int kind, int64_t n, int64_t d, int64_t k, int form) {
              n * (nkb * 128 + 4 * d4 + 8 + 16 + 4) + kp * (nkb * 128 + 32 + 4 * d4) +
              152 * (kp * d4 + kp) * 8;
     }
-    return b + (b >> 4) + (16 << 20);  // allocator slack
+    return b;
 }
 
+int64_t with_slack(int64_t b) { return b + (b >> 4) + (16 << 20); }
+
+// What one replayed request holds while admitted: its data and the server's
+// working memory, with allocator slack.
+int64_t request_bytes(int kind, int64_t n, int64_t d, int64_t k, int form) {
+    return with_slack(data_bytes(kind, n, d, k) + work_bytes(kind, n, d, k, form));
+}
+
+// A replayed request's data (generated on the device when it is admitted).
 struct ReqMem {
     Scratch mem;
     float *X = nullptr, *w = nullptr, *C = nullptr, *Cres = nullptr;
     int32_t *labels = nullptr;
-    float *dist = nullptr;        // transform: (k, n) distances
-    double *partials = nullptr;   // transform: checksum scratch, then the sum
+    float *dist = nullptr;  // transform: (k, n) distances
 };
 
 int alloc_request(ReqMem &m, int64_t n, int64_t d, int64_t k, int kind, cudaStream_t s) {
     const size_t bX = align256(sizeof(float) * n * d), bw = align256(sizeof(float) * n),
                  bC = align256(sizeof(float) * d * k), bl = align256(sizeof(int32_t) * n);
     const size_t bD = kind == 2 ? align256(sizeof(float) * n * k) : 0;
-    const size_t bP = kind == 2 ? align256(sizeof(double) * (sum_partials_size() + 1)) : 0;
-    KMC_TRY(m.mem.alloc(bX + bw + 2 * bC + bl + bD + bP, s));
+    KMC_TRY(m.mem.alloc(bX + bw + 2 * bC + bl + bD, s));
     char *b = m.mem.as<char>();
     m.X = reinterpret_cast<float *>(b);
     m.w = reinterpret_cast<float *>(b + bX);
     m.C = reinterpret_cast<float *>(b + bX + bw);
     m.Cres = reinterpret_cast<float *>(b + bX + bw + bC);
     m.labels = reinterpret_cast<int32_t *>(b + bX + bw + 2 * bC);
-    if (kind == 2) {
-        m.dist = reinterpret_cast<float *>(b + bX + bw + 2 * bC + bl);
-        m.partials = reinterpret_cast<double *>(b + bX + bw + 2 * bC + bl + bD);
-    }
+    if (kind == 2) m.dist = reinterpret_cast<float *>(b + bX + bw + 2 * bC + bl);
     return KMC_OK;
 }
 
-// Float64 total of a transform request's distances (deterministic order).
-int dist_checksum(ReqMem &m, int64_t n, int64_t k, cudaStream_t s, double *out) {
-    double *sum = m.partials + sum_partials_size();
-    KMC_TRY(launch_sum_f64<float>(m.dist, n * k, m.partials, sum, s));
-    KMC_CUDA_TRY(cudaMemcpyAsync(out, sum, sizeof(double), cudaMemcpyDeviceToHost, s));
-    KMC_CUDA_TRY(cudaStreamSynchronize(s));
-    return KMC_OK;
-}
-
+// State of a request while it runs.
 struct Active {
-    int64_t req = -1;
     int64_t inst = -1;                 // plain: batch instance
     std::unique_ptr<FitBase> fit;      // mixed: tensor-core fit session
     cudaEvent_t ev = nullptr;          // mixed: a transform's distances are written
     cudaStream_t st = nullptr;         // the request's stream
-    int stream = 0;
-    int64_t bytes = 0;
-    std::unique_ptr<ReqMem> mem;
+    Scratch sums;                      // transform: float64 checksum scratch
     // mixed fits and predictions: one captured iteration (kernels + a copy of
     // the loop state to pinned host memory), the event that marks the end of
     // the session's last enqueued work, and its pinned result slot
@@ -519,6 +522,7 @@ struct Active {
     ~Active() {
         if (iter_graph) cudaGraphExecDestroy(iter_graph);
         if (step_ev) cudaEventDestroy(step_ev);
+        if (ev) cudaEventDestroy(ev);
     }
 };
 
@@ -553,6 +557,435 @@ int capture_iteration(Active &a) {
     return KMC_OK;
 }
 
+
+// A request server: fits, predictions and transforms of different sizes on
+// caller buffers, admitted in submission order while the HBM budget and the
+// number of running requests allow; predictions wait (without blocking the
+// queue) for the fit whose model they use.  A fit's centroids stay on the
+// device as its model until the ticket is released or the server closed.
+//   plain form   every running request is an instance of one batched engine
+//                (persistent kernels fed by a device work queue, replayed as
+//                CUDA graphs); each progress call advances all of them by one
+//                iteration and retires the finished ones
+//   mixed forms  one tensor-core fit session per request on a pool of
+//                streams; each session replays a captured iteration and
+//                advances on its own (event queries, no host waits)
+// The server is driven by its callers (submit, poll, wait): calls on one
+// server must not overlap.
+struct Server {
+    struct Ticket {
+        int64_t id = -1;
+        int kind = 0;  // 0 fit, 1 predict, 2 transform
+        int state = KMC_REQ_PENDING, status = KMC_OK;
+        int64_t n = 0, d = 0, k = 0, max_iter = 0, model = -1;
+        double tol = 0.0;
+        const float *X = nullptr, *w = nullptr, *Cinit = nullptr;
+        int32_t *labels = nullptr;
+        float *Cout = nullptr, *dist = nullptr;
+        Scratch model_mem;   // fit: working centroids, then the model
+        float *mdl = nullptr;
+        int64_t extra = 0;   // bytes the caller declares held while it runs
+        int64_t bytes = 0;   // bytes admitted
+        cudaEvent_t ready = nullptr;  // the caller's writes of the inputs
+        // replay harness: makes the request's data when it is admitted
+        std::function<int(Ticket &, cudaStream_t)> on_admit;
+        std::unique_ptr<ReqMem> data;
+        double admit_s = -1.0, finish_s = -1.0, inertia = 0.0;
+        int64_t n_iter = 0;
+        bool cancel = false, released = false;
+        std::unique_ptr<Active> act;
+        ~Ticket() {
+            if (ready) cudaEventDestroy(ready);
+        }
+    };
+
+    int form = KMC_FORM_PLAIN;
+    bool plain = true;
+    int64_t budget = 0, max_active = 1, in_use = 0;
+    cudaStream_t user = nullptr;
+    BatchEngine eng;
+    static constexpr int kStreams = 8;
+    std::vector<cudaStream_t> pool;
+    int64_t rr = 0;
+    static constexpr size_t kSlotBytes = 128;
+    char *pinned = nullptr;
+    std::vector<int> free_slots;
+    std::vector<std::unique_ptr<Ticket>> tickets;
+    std::deque<int64_t> pending;
+    std::vector<int64_t> running;
+    std::vector<int64_t> finished_log;  // tickets in the order they finished
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+
+    double elapsed() const {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+
+    ~Server() {
+        // requests still running are stopped; nothing may write memory that
+        // is about to be freed
+        for (int64_t id : running) {
+            Ticket &t = *tickets[(size_t)id];
+            if (t.act && t.act->st) cudaStreamSynchronize(t.act->st);
+            t.act.reset();
+        }
+        if (plain && eng.s) cudaStreamSynchronize(eng.s);
+        for (auto t : pool) cudaStreamSynchronize(t);
+        tickets.clear();
+        for (auto t : pool) {
+            cudaStreamSynchronize(t);
+            cudaStreamDestroy(t);
+        }
+        if (pinned) cudaFreeHost(pinned);
+    }
+
+    int init(int f, int64_t bud, int64_t max_act, cudaStream_t s) {
+        KMC_CHECK_ARG(f == KMC_FORM_PLAIN || f == KMC_FORM_MIXED_BF16 || f == KMC_FORM_MIXED_FP16,
+                      "unknown form %d", f);
+        KMC_CHECK_ARG(bud > 0, "hbm_budget_bytes must be positive");
+        KMC_CHECK_ARG(max_act >= 1 && max_act <= (1 << 16), "max_active out of range");
+        form = f;
+        plain = f == KMC_FORM_PLAIN;
+        budget = bud;
+        max_active = max_act;
+        user = s;
+        if (plain) {
+            KMC_TRY(eng.init(max_act, s));
+        } else {
+            for (int q = 0; q < kStreams; ++q) {
+                cudaStream_t t = nullptr;
+                KMC_CUDA_TRY(cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking));
+                pool.push_back(t);
+            }
+            KMC_CUDA_TRY(cudaHostAlloc(&pinned, kSlotBytes * (size_t)max_act, cudaHostAllocDefault));
+            for (int64_t q = max_act - 1; q >= 0; --q) free_slots.push_back((int)q);
+        }
+        return KMC_OK;
+    }
+
+    Ticket *get(int64_t id) {
+        if (id < 0 || id >= (int64_t)tickets.size() || tickets[(size_t)id]->released)
+            return nullptr;
+        return tickets[(size_t)id].get();
+    }
+
+    // Queues a request; the caller's stream orders its input writes.
+    int submit(std::unique_ptr<Ticket> t, int64_t *id_out) {
+        KMC_CUDA_TRY(cudaEventCreateWithFlags(&t->ready, cudaEventDisableTiming));
+        KMC_CUDA_TRY(cudaEventRecord(t->ready, user));
+        const int64_t id = (int64_t)tickets.size();
+        t->id = id;
+        tickets.push_back(std::move(t));
+        pending.push_back(id);
+        *id_out = id;
+        return KMC_OK;
+    }
+
+    static bool final_state(int s) { return s >= KMC_REQ_DONE; }
+
+    void end(Ticket &t, int state, int status) {
+        if (t.act) {
+            if (t.act->slot >= 0) free_slots.push_back(t.act->slot);
+            t.act.reset();
+        }
+        if (state != KMC_REQ_DONE || t.kind != 0) t.model_mem.release();
+        if (state != KMC_REQ_DONE) t.mdl = nullptr;
+        t.data.reset();
+        in_use -= t.bytes;
+        t.bytes = 0;
+        t.state = state;
+        t.status = status;
+        t.finish_s = elapsed();
+        finished_log.push_back(t.id);
+    }
+
+    // Starts an admitted request: its stream waits for the caller's writes,
+    // the harness makes its data, a fit copies its initial centroids into its
+    // model, and the work is handed to the engine or a fit session.
+    int start(Ticket &t, const Ticket *m) {
+        // owned by the ticket from here on, so a failure below is cleaned up
+        // by end() (the session, the pinned slot)
+        t.act = std::make_unique<Active>();
+        Active *a = t.act.get();
+        a->st = plain ? user : pool[(size_t)(rr++ % kStreams)];
+        KMC_CUDA_TRY(cudaStreamWaitEvent(a->st, t.ready, 0));
+        if (t.on_admit) KMC_TRY(t.on_admit(t, a->st));
+        const float *model = (t.kind == 0) ? nullptr : m->mdl;
+        if (t.kind == 0) {
+            KMC_TRY(t.model_mem.alloc(sizeof(float) * t.d * t.k, a->st));
+            t.mdl = t.model_mem.as<float>();
+            KMC_CUDA_TRY(cudaMemcpyAsync(t.mdl, t.Cinit, sizeof(float) * t.d * t.k,
+                                         cudaMemcpyDeviceToDevice, a->st));
+        }
+        if (t.kind == 2) KMC_TRY(a->sums.alloc(sizeof(double) * (sum_partials_size() + 1), a->st));
+        if (plain) {
+            // the engine's stream is ordered after `user` when an instance is added
+            if (t.kind == 0)
+                KMC_TRY(eng.add(B_FIT, t.X, t.w, t.mdl, t.labels, t.n, t.d, t.k, t.tol,
+                                t.max_iter, &a->inst));
+            else if (t.kind == 1)
+                KMC_TRY(eng.add(B_ASSIGN, t.X, nullptr, const_cast<float *>(model), t.labels, t.n,
+                                t.d, t.k, 0.0, 0, &a->inst));
+            else
+                KMC_TRY(eng.add(B_TRANSFORM, t.X, nullptr, const_cast<float *>(model), nullptr,
+                                t.n, t.d, t.k, 0.0, 0, &a->inst, t.dist));
+        } else if (t.kind == 2) {
+            // exact float32 distances (no tensor-core form of the distance matrix)
+            KMC_TRY(launch_distances<float>(t.X, model, t.dist, t.n, t.d, t.k, a->st));
+            KMC_CUDA_TRY(cudaEventCreateWithFlags(&a->ev, cudaEventDisableTiming));
+            KMC_CUDA_TRY(cudaEventRecord(a->ev, a->st));
+        } else {
+            FitParams<float, int32_t> p;
+            p.X = t.X;
+            p.w = t.kind == 0 ? t.w : nullptr;
+            // a prediction reads the model and writes nothing but labels
+            p.centroids = t.kind == 0 ? t.mdl : const_cast<float *>(model);
+            p.new_centroids = t.kind == 0 ? t.Cout : const_cast<float *>(model);
+            p.labels = t.labels;
+            p.n = t.n;
+            p.d = t.d;
+            p.k = t.k;
+            p.tol = t.kind == 0 ? t.tol : 0.0;
+            p.max_iter = t.kind == 0 ? t.max_iter : 0;
+            p.stream = a->st;
+            KMC_TRY(make_mixed_fit<float, int32_t>(p, form, &a->fit));
+            a->slot = free_slots.back();
+            free_slots.pop_back();
+            a->hstate = reinterpret_cast<LoopState *>(pinned + kSlotBytes * (size_t)a->slot);
+            a->hinertia = reinterpret_cast<double *>(pinned + kSlotBytes * (size_t)a->slot + 64);
+            // the slot's previous session has retired: nothing writes it now
+            *reinterpret_cast<volatile int *>(&a->hstate->done) = 0;
+            *reinterpret_cast<volatile unsigned *>(&a->hstate->err) = 0u;
+            KMC_CUDA_TRY(cudaEventCreateWithFlags(&a->step_ev, cudaEventDisableTiming));
+            if (p.max_iter > 0) KMC_TRY(capture_iteration(*a));
+        }
+        return KMC_OK;
+    }
+
+    // Admission in submission order while the budget and the running count
+    // allow; a prediction whose model is not ready yet waits without
+    // blocking the requests behind it.
+    int admit(bool *moved) {
+        for (auto it = pending.begin(); it != pending.end();) {
+            const int64_t id = *it;
+            Ticket &t = *tickets[(size_t)id];
+            if (t.cancel) {
+                end(t, KMC_REQ_CANCELLED, KMC_ERR_CANCELLED);
+                it = pending.erase(it);
+                *moved = true;
+                continue;
+            }
+            const Ticket *m = nullptr;
+            if (t.kind != 0) {
+                m = tickets[(size_t)t.model].get();
+                if (m->state == KMC_REQ_PENDING || m->state == KMC_REQ_RUNNING) {
+                    ++it;
+                    continue;
+                }
+                if (m->state != KMC_REQ_DONE || m->released) {
+                    set_error("request %lld: its model (request %lld) did not complete",
+                              (long long)id, (long long)t.model);
+                    end(t, KMC_REQ_FAILED, KMC_ERR_INVALID_ARGUMENT);
+                    it = pending.erase(it);
+                    *moved = true;
+                    continue;
+                }
+            }
+            const int64_t need = with_slack(work_bytes(t.kind, t.n, t.d, t.k, form) + t.extra);
+            if (need > budget) {  // can never be admitted
+                end(t, KMC_REQ_FAILED, KMC_ERR_OUT_OF_MEMORY);
+                it = pending.erase(it);
+                *moved = true;
+                continue;
+            }
+            if ((int64_t)running.size() >= max_active || in_use + need > budget) break;
+            it = pending.erase(it);
+            t.bytes = need;
+            in_use += need;
+            t.state = KMC_REQ_RUNNING;
+            t.admit_s = elapsed();
+            const int rc = start(t, m);
+            *moved = true;
+            if (rc != KMC_OK) {
+                // a request that cannot start fails alone; the server goes on
+                if (t.act && t.act->st) cudaStreamSynchronize(t.act->st);
+                if (plain && t.act && t.act->inst >= 0) eng.remove(t.act->inst);
+                end(t, KMC_REQ_FAILED, rc);
+                continue;
+            }
+            running.push_back(id);
+        }
+        return KMC_OK;
+    }
+
+    // Float64 total of a transform's distances (deterministic order).
+    int dist_checksum(Ticket &t, cudaStream_t s, double *out) {
+        double *part = t.act->sums.as<double>();
+        KMC_TRY(launch_sum_f64<float>(t.dist, t.n * t.k, part, part + sum_partials_size(), s));
+        KMC_CUDA_TRY(cudaMemcpyAsync(out, part + sum_partials_size(), sizeof(double),
+                                     cudaMemcpyDeviceToHost, s));
+        KMC_CUDA_TRY(cudaStreamSynchronize(s));
+        return KMC_OK;
+    }
+
+    // Plain form: one engine iteration for every running request.
+    int advance_plain(bool *moved) {
+        if (running.empty()) return KMC_OK;
+        KMC_TRY(eng.step(nullptr));
+        *moved = true;
+        for (size_t r = 0; r < running.size();) {
+            Ticket &t = *tickets[(size_t)running[r]];
+            const int64_t q = t.act->inst;
+            int state = -1, status = KMC_OK;
+            if (t.cancel) {
+                state = KMC_REQ_CANCELLED;
+                status = KMC_ERR_CANCELLED;
+            } else if (eng.state[(size_t)q] == BatchEngine::FINISHED) {
+                state = KMC_REQ_DONE;
+                t.n_iter = eng.res_iter[(size_t)q];
+                t.inertia = eng.res_inertia[(size_t)q];
+                if (t.kind == 0 && t.Cout != nullptr)
+                    KMC_CUDA_TRY(cudaMemcpyAsync(t.Cout, t.mdl, sizeof(float) * t.d * t.k,
+                                                 cudaMemcpyDeviceToDevice, eng.s));
+                if (t.kind == 2) KMC_TRY(dist_checksum(t, eng.s, &t.inertia));
+                KMC_CUDA_TRY(cudaStreamSynchronize(eng.s));
+            }
+            if (state < 0) {
+                ++r;
+                continue;
+            }
+            KMC_TRY(eng.remove(q));
+            end(t, state, status);
+            running.erase(running.begin() + (int64_t)r);
+        }
+        return KMC_OK;
+    }
+
+    // Mixed forms: each session advances on its own.  Once its last enqueued
+    // work is done it gets kItersPerVisit more iterations (one graph launch
+    // each) or, when its loop has stopped, the final pass, and it retires when
+    // that is done.  No session waits for another, and the host neither
+    // launches kernels one by one nor waits on a stream.
+    int advance_mixed(bool *moved) {
+        for (size_t r = 0; r < running.size();) {
+            Ticket &t = *tickets[(size_t)running[r]];
+            Active &a = *t.act;
+            auto retire = [&](int state, int status) {
+                end(t, state, status);
+                running.erase(running.begin() + (int64_t)r);
+                *moved = true;
+            };
+            if (!a.fit) {  // a transform in flight
+                const cudaError_t q = cudaEventQuery(a.ev);
+                if (q == cudaErrorNotReady) {
+                    ++r;
+                    continue;
+                }
+                KMC_CUDA_TRY(q);
+                if (!t.cancel) KMC_TRY(dist_checksum(t, a.st, &t.inertia));
+                retire(t.cancel ? KMC_REQ_CANCELLED : KMC_REQ_DONE,
+                       t.cancel ? KMC_ERR_CANCELLED : KMC_OK);
+                continue;
+            }
+            if (a.inflight) {
+                const cudaError_t q = cudaEventQuery(a.step_ev);
+                if (q == cudaErrorNotReady) {
+                    ++r;
+                    continue;
+                }
+                KMC_CUDA_TRY(q);
+                a.inflight = false;
+            }
+            if (t.cancel) {
+                retire(KMC_REQ_CANCELLED, KMC_ERR_CANCELLED);
+                continue;
+            }
+            const volatile LoopState *hs = a.hstate;
+            if (a.final_enqueued) {
+                t.n_iter = (int64_t)hs->n_iter;
+                t.inertia = *(const volatile double *)a.hinertia;
+                // a tensor-core kernel that gave up a wait fails the request
+                if (hs->err != 0)
+                    retire(KMC_REQ_FAILED, KMC_ERR_DEVICE_TIMEOUT);
+                else
+                    retire(KMC_REQ_DONE, KMC_OK);
+                continue;
+            }
+            if (a.iter_graph == nullptr || hs->done) {
+                KMC_TRY(a.fit->finalize_enqueue(a.hstate, a.hinertia));
+                a.final_enqueued = true;
+            } else {
+                for (int i = 0; i < kItersPerVisit; ++i)
+                    KMC_CUDA_TRY(cudaGraphLaunch(a.iter_graph, a.st));
+            }
+            KMC_CUDA_TRY(cudaEventRecord(a.step_ev, a.st));
+            a.inflight = true;
+            *moved = true;
+            ++r;
+        }
+        return KMC_OK;
+    }
+
+    int progress(bool *moved) {
+        *moved = false;
+        KMC_TRY(admit(moved));
+        if (plain)
+            KMC_TRY(advance_plain(moved));
+        else
+            KMC_TRY(advance_mixed(moved));
+        // retirements free budget: admit again without waiting for the next call
+        if (*moved) KMC_TRY(admit(moved));
+        return KMC_OK;
+    }
+
+    int wait(int64_t id) {
+        Ticket *t = get(id);
+        KMC_CHECK_ARG(t != nullptr, "no such ticket %lld", (long long)id);
+        while (!final_state(t->state)) {
+            bool moved = false;
+            KMC_TRY(progress(&moved));
+            if (!moved) std::this_thread::sleep_for(std::chrono::microseconds(20));
+        }
+        return KMC_OK;
+    }
+
+    int cancel(int64_t id) {
+        Ticket *t = get(id);
+        KMC_CHECK_ARG(t != nullptr, "no such ticket %lld", (long long)id);
+        if (!final_state(t->state)) t->cancel = true;
+        bool moved = false;
+        return progress(&moved);
+    }
+
+    // Drops a finished request's record and, for a fit, its model.
+    int release(int64_t id) {
+        Ticket *t = get(id);
+        KMC_CHECK_ARG(t != nullptr, "no such ticket %lld", (long long)id);
+        KMC_CHECK_ARG(final_state(t->state), "ticket %lld has not finished", (long long)id);
+        t->model_mem.release();
+        t->mdl = nullptr;
+        t->released = true;
+        return KMC_OK;
+    }
+};
+
+
+// Shapes a form can serve: the batched engine takes d <= 1024 and k <= 4096;
+// the tensor-core sessions take what the mixed fit supports.
+int check_shape(int form, int64_t d, int64_t k) {
+    if (form == KMC_FORM_PLAIN) {
+        KMC_CHECK_ARG(d <= 1024 && k <= 4096, "the plain server takes d <= 1024 and k <= 4096");
+        return KMC_OK;
+    }
+    if (!mixed_fit_supported(d, k)) {
+        set_error("the mixed forms do not support d=%lld, k=%lld", (long long)d, (long long)k);
+        return KMC_ERR_UNSUPPORTED;
+    }
+    return KMC_OK;
+}
+
+// Replays a request stream on a Server: each request is submitted at its
+// arrival time and its data (seeded blobs, a seeded-row initialisation) is
+// generated on the device when it is admitted, so the budget covers it.
 int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t budget,
               int64_t max_active, cudaStream_t s, kmc_serve_result_t *out, double *makespan) {
     KMC_CHECK_ARG(n_req >= 0 && (n_req == 0 || (rq != nullptr && out != nullptr)),
@@ -578,276 +1011,85 @@ int serve_run(const kmc_serve_request_t *rq, int64_t n_req, int form, int64_t bu
                       (long long)r);
         out[r] = kmc_serve_result_t{-1.0, -1.0, 0, 0.0, KMC_OK, 0};
     }
-    using clk = std::chrono::steady_clock;
-    const auto t0 = clk::now();
-    auto elapsed = [&]() { return std::chrono::duration<double>(clk::now() - t0).count(); };
-
-    const bool plain = form == KMC_FORM_PLAIN;
-    BatchEngine eng;
-    if (plain) KMC_TRY(eng.init(max_active, s));
-    constexpr int kStreams = 8;
-    std::vector<cudaStream_t> pool;
-    if (!plain) {
-        for (int q = 0; q < kStreams; ++q) {
-            cudaStream_t t = nullptr;
-            KMC_CUDA_TRY(cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking));
-            pool.push_back(t);
-        }
-    }
-    struct PoolGuard {
-        std::vector<cudaStream_t> &p;
-        ~PoolGuard() {
-            for (auto t : p) {
-                cudaStreamSynchronize(t);
-                cudaStreamDestroy(t);
-            }
-        }
-    } pool_guard{pool};
-    // pinned result slots of the mixed sessions (loop state, inertia total)
-    constexpr size_t kSlotBytes = 128;
-    const int64_t n_slots = plain ? 0 : std::max<int64_t>(1, std::min<int64_t>(max_active, n_req));
-    char *pinned = nullptr;
-    std::vector<int> free_slots;
-    if (!plain) {
-        KMC_CUDA_TRY(cudaHostAlloc(&pinned, kSlotBytes * (size_t)n_slots, cudaHostAllocDefault));
-        for (int64_t q = n_slots - 1; q >= 0; --q) free_slots.push_back((int)q);
-    }
-    struct PinnedGuard {
-        char *p;
-        std::vector<cudaStream_t> &streams;
-        ~PinnedGuard() {  // runs before the stream pool is destroyed
-            for (auto t : streams) cudaStreamSynchronize(t);
-            if (p) cudaFreeHost(p);
-        }
-    } pinned_guard{pinned, pool};
-
-    std::vector<std::vector<float>> models((size_t)n_req);
-    std::vector<char> model_ready((size_t)n_req, 0);
-    std::deque<int64_t> pending;
-    std::vector<std::unique_ptr<Active>> active;
-    int64_t next = 0, finished = 0, in_use = 0, rr = 0;
-
-    auto finish = [&](Active &a, int64_t n_iter, double inertia, int status) -> int {
-        const kmc_serve_request_t &q = rq[a.req];
-        kmc_serve_result_t &o = out[a.req];
-        if (status == KMC_OK && q.kind == 2)
-            KMC_TRY(dist_checksum(*a.mem, q.n_samples, q.n_clusters, a.st, &inertia));
-        if (a.ev) {
-            cudaEventDestroy(a.ev);
-            a.ev = nullptr;
-        }
-        if (status == KMC_OK && q.kind == 0) {
-            std::vector<float> &m = models[(size_t)a.req];
-            m.resize((size_t)(q.n_features * q.n_clusters));
-            const float *src = plain ? a.mem->C : a.mem->Cres;
-            KMC_CUDA_TRY(cudaMemcpy(m.data(), src, sizeof(float) * m.size(),
-                                    cudaMemcpyDeviceToHost));
-            model_ready[(size_t)a.req] = 1;
-        }
-        o.finish_s = elapsed();
-        o.n_iter = n_iter;
-        o.inertia = inertia;
-        o.status = status;
-        in_use -= a.bytes;
-        ++finished;
-        if (a.slot >= 0) {
-            free_slots.push_back(a.slot);
-            a.slot = -1;
-        }
-        return KMC_OK;
-    };
-
-    auto admit = [&](int64_t r, int64_t bytes) -> int {
-        const kmc_serve_request_t &q = rq[r];
-        auto a = std::make_unique<Active>();
-        a->req = r;
-        a->bytes = bytes;
-        a->mem = std::make_unique<ReqMem>();
-        const int64_t n = q.n_samples, d = q.n_features, k = q.n_clusters;
-        cudaStream_t st = plain ? s : pool[(size_t)(rr++ % kStreams)];
-        a->stream = plain ? 0 : (int)((rr - 1) % kStreams);
-        a->st = st;
-        KMC_TRY(alloc_request(*a->mem, n, d, k, q.kind, st));
-        ReqMem &m = *a->mem;
-        KMC_TRY(launch_blobs(m.X, n, d, q.n_centers, -10.f, 10.f, q.std_lo, q.std_hi, q.seed, st));
-        KMC_TRY(launch_fill<float>(m.w, 1.f, n, st));
-        if (q.kind == 0) {
-            std::vector<int32_t> rows;
-            seeded_rows(n, k, q.seed ^ 0x9999ull, &rows);
-            Scratch idx;
-            KMC_TRY(idx.alloc(sizeof(int32_t) * rows.size(), st));
-            KMC_CUDA_TRY(cudaMemcpyAsync(idx.ptr, rows.data(), sizeof(int32_t) * rows.size(),
-                                         cudaMemcpyHostToDevice, st));
-            KMC_TRY(launch_gather_rows(m.X, n, d, idx.as<int32_t>(), k, m.C, st));
-            // (a pageable upload returns once its source is staged, and the
-            // index buffer is freed in stream order: the mixed sessions need
-            // no wait here)
-            if (plain) KMC_CUDA_TRY(cudaStreamSynchronize(st));
-        } else {
-            const std::vector<float> &mdl = models[(size_t)q.model];
-            KMC_CUDA_TRY(cudaMemcpyAsync(m.C, mdl.data(), sizeof(float) * mdl.size(),
-                                         cudaMemcpyHostToDevice, st));
-            if (plain) KMC_CUDA_TRY(cudaStreamSynchronize(st));
-        }
-        out[r].admit_s = elapsed();
-        if (plain) {
-            if (q.kind == 0)
-                KMC_TRY(eng.add(B_FIT, m.X, m.w, m.C, m.labels, n, d, k, q.tol, q.max_iter,
-                                &a->inst));
-            else if (q.kind == 1)
-                KMC_TRY(eng.add(B_ASSIGN, m.X, nullptr, m.C, m.labels, n, d, k, 0.0, 0, &a->inst));
-            else
-                KMC_TRY(eng.add(B_TRANSFORM, m.X, nullptr, m.C, nullptr, n, d, k, 0.0, 0,
-                                &a->inst, m.dist));
-        } else if (q.kind == 2) {
-            // exact float32 distances (no tensor-core form of the distance
-            // matrix), on the request's stream
-            KMC_TRY(launch_distances<float>(m.X, m.C, m.dist, n, d, k, st));
-            KMC_CUDA_TRY(cudaEventCreateWithFlags(&a->ev, cudaEventDisableTiming));
-            KMC_CUDA_TRY(cudaEventRecord(a->ev, st));
-        } else {
-            FitParams<float, int32_t> p;
-            p.X = m.X;
-            p.w = m.w;
-            p.centroids = m.C;
-            p.new_centroids = m.Cres;
-            p.labels = m.labels;
-            p.n = n;
-            p.d = d;
-            p.k = k;
-            p.tol = q.kind == 0 ? q.tol : 0.0;
-            p.max_iter = q.kind == 0 ? q.max_iter : 0;
-            p.stream = st;
-            KMC_TRY(make_mixed_fit<float, int32_t>(p, form, &a->fit));
-            a->slot = free_slots.back();
-            free_slots.pop_back();
-            a->hstate = reinterpret_cast<LoopState *>(pinned + kSlotBytes * (size_t)a->slot);
-            a->hinertia = reinterpret_cast<double *>(pinned + kSlotBytes * (size_t)a->slot + 64);
-            // the slot's previous session has retired: nothing writes it now
-            *reinterpret_cast<volatile int *>(&a->hstate->done) = 0;
-            KMC_CUDA_TRY(cudaEventCreateWithFlags(&a->step_ev, cudaEventDisableTiming));
-            if (p.max_iter > 0) KMC_TRY(capture_iteration(*a));
-        }
-        in_use += bytes;
-        active.push_back(std::move(a));
-        return KMC_OK;
-    };
-
+    Server srv;
+    KMC_TRY(srv.init(form, budget, max_active, s));
+    std::vector<int64_t> ticket(n_req, -1), req_of;
+    int64_t next = 0, finished = 0;
+    size_t seen = 0;
     while (finished < n_req) {
-        const double now = elapsed();
-        while (next < n_req && rq[next].arrival_s <= now) pending.push_back(next++);
-        // admission in arrival order; predictions wait (without blocking the
-        // queue) until their model has been fitted
-        for (auto it = pending.begin(); it != pending.end();) {
-            const kmc_serve_request_t &q = rq[*it];
-            if (q.kind != 0 && !model_ready[(size_t)q.model]) {
-                ++it;
-                continue;
-            }
-            const int64_t need = request_bytes(q.kind, q.n_samples, q.n_features, q.n_clusters,
-                                               form);
-            if (need > budget) {  // can never be admitted
-                out[*it].status = KMC_ERR_OUT_OF_MEMORY;
-                out[*it].finish_s = elapsed();
-                ++finished;
-                it = pending.erase(it);
-                continue;
-            }
-            if ((int64_t)active.size() >= max_active || in_use + need > budget) break;
-            KMC_TRY(admit(*it, need));
-            it = pending.erase(it);
+        const double now = srv.elapsed();
+        while (next < n_req && rq[next].arrival_s <= now) {
+            const kmc_serve_request_t &q = rq[next];
+            auto t = std::make_unique<Server::Ticket>();
+            t->kind = q.kind;
+            t->n = q.n_samples;
+            t->d = q.n_features;
+            t->k = q.n_clusters;
+            t->tol = q.kind == 0 ? q.tol : 0.0;
+            t->max_iter = q.kind == 0 ? q.max_iter : 0;
+            t->model = q.kind == 0 ? -1 : ticket[(size_t)q.model];
+            t->extra = data_bytes(q.kind, q.n_samples, q.n_features, q.n_clusters);
+            t->on_admit = [q](Server::Ticket &tk, cudaStream_t st) -> int {
+                tk.data = std::make_unique<ReqMem>();
+                ReqMem &m = *tk.data;
+                KMC_TRY(alloc_request(m, tk.n, tk.d, tk.k, q.kind, st));
+                KMC_TRY(launch_blobs(m.X, tk.n, tk.d, q.n_centers, -10.f, 10.f, q.std_lo,
+                                     q.std_hi, q.seed, st));
+                KMC_TRY(launch_fill<float>(m.w, 1.f, tk.n, st));
+                if (q.kind == 0) {
+                    std::vector<int32_t> rows;
+                    seeded_rows(tk.n, tk.k, q.seed ^ 0x9999ull, &rows);
+                    Scratch idx;
+                    KMC_TRY(idx.alloc(sizeof(int32_t) * rows.size(), st));
+                    // a pageable upload returns once its source is staged, and
+                    // the index buffer is freed in stream order
+                    KMC_CUDA_TRY(cudaMemcpyAsync(idx.ptr, rows.data(),
+                                                 sizeof(int32_t) * rows.size(),
+                                                 cudaMemcpyHostToDevice, st));
+                    KMC_TRY(launch_gather_rows(m.X, tk.n, tk.d, idx.as<int32_t>(), tk.k, m.C, st));
+                }
+                tk.X = m.X;
+                tk.w = m.w;
+                tk.Cinit = m.C;
+                tk.labels = m.labels;
+                tk.Cout = m.Cres;
+                tk.dist = m.dist;
+                return KMC_OK;
+            };
+            int64_t id = -1;
+            KMC_TRY(srv.submit(std::move(t), &id));
+            ticket[(size_t)next] = id;
+            if ((int64_t)req_of.size() <= id) req_of.resize((size_t)id + 1, -1);
+            req_of[(size_t)id] = next;
+            ++next;
         }
-        if (active.empty()) {
-            if (next < n_req) {
-                const double wait = rq[next].arrival_s - elapsed();
-                if (wait > 0)
-                    std::this_thread::sleep_for(
-                        std::chrono::microseconds((int64_t)(std::min(wait, 0.001) * 1e6)));
-            } else if (!pending.empty()) {
-                // only predictions whose model failed remain
-                for (int64_t r : pending) {
-                    out[r].status = KMC_ERR_INVALID_ARGUMENT;
-                    out[r].finish_s = elapsed();
-                    ++finished;
-                }
-                pending.clear();
-            }
-            continue;
+        bool moved = false;
+        KMC_TRY(srv.progress(&moved));
+        for (; seen < srv.finished_log.size(); ++seen) {
+            const int64_t id = srv.finished_log[seen];
+            const Server::Ticket &t = *srv.tickets[(size_t)id];
+            kmc_serve_result_t &o = out[(size_t)req_of[(size_t)id]];
+            o.admit_s = t.admit_s;
+            o.finish_s = t.finish_s;
+            o.n_iter = t.n_iter;
+            o.inertia = t.inertia;
+            o.status = t.status;
+            ++finished;
         }
-        if (plain) {
-            KMC_TRY(eng.step(nullptr));
-            for (size_t t = 0; t < active.size();) {
-                Active &a = *active[t];
-                if (eng.state[(size_t)a.inst] == BatchEngine::FINISHED) {
-                    KMC_TRY(finish(a, eng.res_iter[(size_t)a.inst], eng.res_inertia[(size_t)a.inst],
-                                   KMC_OK));
-                    KMC_TRY(eng.remove(a.inst));
-                    active.erase(active.begin() + (int64_t)t);
-                } else {
-                    ++t;
-                }
-            }
-        } else {
-            // Each session advances on its own: once its last enqueued work is
-            // done it gets kItersPerVisit more iterations (one graph launch
-            // each) or, when its loop has stopped, the final pass, and it
-            // retires when that is done.  No step waits for the slowest
-            // session, and the host neither launches kernels one by one nor
-            // waits on a stream.
-            bool progressed = false;
-            for (size_t t = 0; t < active.size();) {
-                Active &a = *active[t];
-                if (!a.fit) {  // a transform in flight
-                    const cudaError_t q = cudaEventQuery(a.ev);
-                    if (q == cudaErrorNotReady) {
-                        ++t;
-                        continue;
-                    }
-                    KMC_CUDA_TRY(q);
-                    KMC_TRY(finish(a, 0, 0.0, KMC_OK));
-                    active.erase(active.begin() + (int64_t)t);
-                    progressed = true;
-                    continue;
-                }
-                if (a.inflight) {
-                    const cudaError_t q = cudaEventQuery(a.step_ev);
-                    if (q == cudaErrorNotReady) {
-                        ++t;
-                        continue;
-                    }
-                    KMC_CUDA_TRY(q);
-                    a.inflight = false;
-                }
-                const volatile LoopState *hs = a.hstate;
-                if (a.final_enqueued) {
-                    // a tensor-core kernel that gave up a wait marks the request failed
-                    KMC_TRY(finish(a, (int64_t)hs->n_iter, *(const volatile double *)a.hinertia,
-                                   hs->err != 0 ? KMC_ERR_DEVICE_TIMEOUT : KMC_OK));
-                    a.fit.reset();
-                    active.erase(active.begin() + (int64_t)t);
-                    progressed = true;
-                    continue;
-                }
-                if (a.iter_graph == nullptr || hs->done) {
-                    KMC_TRY(a.fit->finalize_enqueue(a.hstate, a.hinertia));
-                    a.final_enqueued = true;
-                } else {
-                    for (int r = 0; r < kItersPerVisit; ++r)
-                        KMC_CUDA_TRY(cudaGraphLaunch(a.iter_graph, a.st));
-                }
-                KMC_CUDA_TRY(cudaEventRecord(a.step_ev, a.st));
-                a.inflight = true;
-                progressed = true;
-                ++t;
-            }
-            if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
+        if (!moved && finished < n_req) {
+            double wait = 20e-6;
+            if (srv.running.empty() && srv.pending.empty() && next < n_req)
+                wait = std::min(std::max(rq[next].arrival_s - srv.elapsed(), 0.0), 0.001);
+            if (wait > 0)
+                std::this_thread::sleep_for(std::chrono::microseconds((int64_t)(wait * 1e6)));
         }
     }
-    if (makespan) *makespan = elapsed();
+    if (makespan) *makespan = srv.elapsed();
     return KMC_OK;
 }
 
-}  // namespace
+}  // namespace serving
+
 
 }  // namespace kmc
 
@@ -855,6 +1097,10 @@ using namespace kmc;
 
 struct kmc_batch_s {
     BatchEngine eng;
+};
+
+struct kmc_server_s {
+    serving::Server srv;
 };
 
 extern "C" {
@@ -970,14 +1216,155 @@ int kmc_serve_bytes_needed(int32_t kind, int64_t n_samples, int64_t n_features,
     KMC_CHECK_ARG(bytes_out != nullptr, "null output");
     KMC_CHECK_ARG(kind >= 0 && kind <= 2, "kind must be 0 (fit), 1 (predict) or 2 (transform)");
     KMC_CHECK_ARG(n_samples >= 0 && n_features >= 1 && n_clusters >= 1, "invalid sizes");
-    *bytes_out = request_bytes(kind, n_samples, n_features, n_clusters, form);
+    *bytes_out = serving::request_bytes(kind, n_samples, n_features, n_clusters, form);
     return KMC_OK;
+}
+
+int kmc_server_open(int form, int64_t hbm_budget_bytes, int64_t max_active, kmc_stream_t stream,
+                    kmc_server_t *server_out) {
+    KMC_CHECK_ARG(server_out != nullptr, "null output handle");
+    auto srv = std::make_unique<kmc_server_s>();
+    KMC_TRY(srv->srv.init(form, hbm_budget_bytes, max_active,
+                          reinterpret_cast<cudaStream_t>(stream)));
+    *server_out = srv.release();
+    return KMC_OK;
+}
+
+int kmc_server_submit_fit_f32(kmc_server_t server, const float *X_t, const float *sample_weight,
+                              const float *init_centroids_t, int32_t *labels_out,
+                              float *centroids_out, int64_t n_samples, int64_t n_features,
+                              int64_t n_clusters, double tol, int64_t max_iter,
+                              int64_t *ticket_out) {
+    KMC_CHECK_ARG(server != nullptr && ticket_out != nullptr, "null argument");
+    KMC_CHECK_ARG(n_samples >= 1 && n_features >= 1 && n_clusters >= 1,
+                  "invalid sizes (n=%lld, d=%lld, k=%lld)", (long long)n_samples,
+                  (long long)n_features, (long long)n_clusters);
+    KMC_CHECK_ARG(n_clusters <= n_samples, "n_clusters exceeds n_samples");
+    KMC_CHECK_ARG(n_samples < (int64_t(1) << 31), "n_samples must fit int32 labels");
+    KMC_CHECK_ARG(tol >= 0.0, "Tolerance must be non-negative");
+    KMC_CHECK_ARG(max_iter >= 0, "max_iter must be non-negative");
+    KMC_CHECK_ARG(X_t != nullptr && sample_weight != nullptr && init_centroids_t != nullptr &&
+                      labels_out != nullptr && centroids_out != nullptr,
+                  "null buffer");
+    KMC_TRY(serving::check_shape(server->srv.form, n_features, n_clusters));
+    auto t = std::make_unique<serving::Server::Ticket>();
+    t->kind = 0;
+    t->n = n_samples;
+    t->d = n_features;
+    t->k = n_clusters;
+    t->tol = tol;
+    t->max_iter = max_iter;
+    t->X = X_t;
+    t->w = sample_weight;
+    t->Cinit = init_centroids_t;
+    t->labels = labels_out;
+    t->Cout = centroids_out;
+    return server->srv.submit(std::move(t), ticket_out);
+}
+
+// Predictions and transforms against the model of an earlier fit ticket.
+static int submit_with_model(kmc_server_t server, int kind, const float *X_t,
+                             int64_t model_ticket, int32_t *labels_out, float *distances_out,
+                             int64_t n_samples, int64_t *ticket_out) {
+    KMC_CHECK_ARG(server != nullptr && ticket_out != nullptr, "null argument");
+    KMC_CHECK_ARG(n_samples >= 1 && n_samples < (int64_t(1) << 31), "invalid n_samples");
+    KMC_CHECK_ARG(X_t != nullptr, "null buffer");
+    const serving::Server::Ticket *m = server->srv.get(model_ticket);
+    KMC_CHECK_ARG(m != nullptr && m->kind == 0, "model_ticket %lld is not a fit of this server",
+                  (long long)model_ticket);
+    auto t = std::make_unique<serving::Server::Ticket>();
+    t->kind = kind;
+    t->n = n_samples;
+    t->d = m->d;
+    t->k = m->k;
+    t->model = model_ticket;
+    t->X = X_t;
+    t->labels = labels_out;
+    t->dist = distances_out;
+    return server->srv.submit(std::move(t), ticket_out);
+}
+
+int kmc_server_submit_predict_f32(kmc_server_t server, const float *X_t, int64_t model_ticket,
+                                  int32_t *labels_out, int64_t n_samples, int64_t *ticket_out) {
+    KMC_CHECK_ARG(labels_out != nullptr, "null labels");
+    return submit_with_model(server, 1, X_t, model_ticket, labels_out, nullptr, n_samples,
+                             ticket_out);
+}
+
+int kmc_server_submit_transform_f32(kmc_server_t server, const float *X_t, int64_t model_ticket,
+                                    float *distances_out, int64_t n_samples,
+                                    int64_t *ticket_out) {
+    KMC_CHECK_ARG(distances_out != nullptr, "null distances");
+    return submit_with_model(server, 2, X_t, model_ticket, nullptr, distances_out, n_samples,
+                             ticket_out);
+}
+
+static void ticket_result(const serving::Server::Ticket &t, int *status_out, int64_t *n_iter_out,
+                          double *inertia_out) {
+    if (status_out) *status_out = t.status;
+    if (n_iter_out) *n_iter_out = t.n_iter;
+    if (inertia_out) *inertia_out = t.inertia;
+}
+
+int kmc_server_poll(kmc_server_t server, int64_t ticket, int *state_out, int *status_out,
+                    int64_t *n_iter_out, double *inertia_out) {
+    KMC_CHECK_ARG(server != nullptr, "null server");
+    KMC_CHECK_ARG(server->srv.get(ticket) != nullptr, "no such ticket %lld", (long long)ticket);
+    bool moved = false;
+    KMC_TRY(server->srv.progress(&moved));
+    const serving::Server::Ticket &t = *server->srv.get(ticket);
+    if (state_out) *state_out = t.state;
+    ticket_result(t, status_out, n_iter_out, inertia_out);
+    return KMC_OK;
+}
+
+int kmc_server_wait(kmc_server_t server, int64_t ticket, int *status_out, int64_t *n_iter_out,
+                    double *inertia_out) {
+    KMC_CHECK_ARG(server != nullptr, "null server");
+    KMC_TRY(server->srv.wait(ticket));
+    ticket_result(*server->srv.get(ticket), status_out, n_iter_out, inertia_out);
+    return KMC_OK;
+}
+
+int kmc_server_cancel(kmc_server_t server, int64_t ticket) {
+    KMC_CHECK_ARG(server != nullptr, "null server");
+    return server->srv.cancel(ticket);
+}
+
+int kmc_server_release(kmc_server_t server, int64_t ticket) {
+    KMC_CHECK_ARG(server != nullptr, "null server");
+    return server->srv.release(ticket);
+}
+
+int kmc_server_stats(kmc_server_t server, int64_t *pending_out, int64_t *running_out,
+                     int64_t *bytes_in_use_out) {
+    KMC_CHECK_ARG(server != nullptr, "null server");
+    if (pending_out) *pending_out = (int64_t)server->srv.pending.size();
+    if (running_out) *running_out = (int64_t)server->srv.running.size();
+    if (bytes_in_use_out) *bytes_in_use_out = server->srv.in_use;
+    return KMC_OK;
+}
+
+int kmc_server_close(kmc_server_t server) {
+    if (server == nullptr) return KMC_OK;
+    int rc = KMC_OK;
+    // requests not yet finished are cancelled; running ones stop after the
+    // work they have in flight
+    for (auto &t : server->srv.tickets)
+        if (!serving::Server::final_state(t->state)) t->cancel = true;
+    while (rc == KMC_OK && (!server->srv.running.empty() || !server->srv.pending.empty())) {
+        bool moved = false;
+        rc = server->srv.progress(&moved);
+        if (!moved) std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+    delete server;
+    return rc;
 }
 
 int kmc_serve_run(const kmc_serve_request_t *requests, int64_t n_requests, int form,
                   int64_t hbm_budget_bytes, int64_t max_active, kmc_stream_t stream,
                   kmc_serve_result_t *results_out, double *makespan_s_out) {
-    return serve_run(requests, n_requests, form, hbm_budget_bytes, max_active,
+    return serving::serve_run(requests, n_requests, form, hbm_budget_bytes, max_active,
                      reinterpret_cast<cudaStream_t>(stream), results_out, makespan_s_out);
 }
 
