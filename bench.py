@@ -387,7 +387,8 @@ def _roofline(workload, form, n, d, k, kern_ms, clocks, sm_count, f64=False):
     flops = 2.0 * n * k * d
     achieved = flops / (kern_ms * 1e-3) / 1e12
     if f64:
-        r = {"bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+        peak = FP64_NOMINAL_TFLOPS
+        r = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
              "peak_source": "nominal dense FP64 rate of a GB300 (no measured FP64 peak); the "
                             "plain float64 form runs on the FP64 pipe",
              "kernel": "tile_kernel (exact fused assignment + accumulation, float64)"}

@@ -417,7 +417,8 @@ int kmc_lloyd_driver_f64_i64(const double *X_t, const double *sample_weight,
  * device; kmc_fit_step enqueues iterations without host synchronisation (the
  * GPU stops the loop itself once tol or max_iter is reached).
  * form: KMC_FORM_PLAIN (exact dataT arithmetic, the reference's) or a mixed
- * tensor-core form (float32 data only). */
+ * tensor-core form (float32 data, n_features <= 256, any n_clusters; the
+ * labels are the exact float32 ones, KMC_ERR_UNSUPPORTED beyond 256 features). */
 typedef struct kmc_fit_s *kmc_fit_t;
 #define KMC_FORM_PLAIN 0
 #define KMC_FORM_MIXED_BF16 1

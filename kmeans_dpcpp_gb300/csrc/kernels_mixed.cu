@@ -129,6 +129,14 @@ struct MixedArgs {
     int stall;         // test of the timeout path: the epilogue first waits on a
                        // barrier that nothing completes
     LoopState *state;  // receives the error bit and stops the loop (nullable)
+    // Column passes (n_clusters beyond what one launch holds in shared
+    // memory): this launch covers columns col0 .. col0 + NCH*256 - 1 of a
+    // global centroid image of k_img rows.  With multi set it writes, per
+    // sample, its best score of the pass (pmax) and full candidate masks of
+    // the pass (cand) instead of labels; a combine kernel decides.
+    int64_t k_img, col0;
+    int multi;
+    float *pmax;
 };
 
 struct SmemLayout {
@@ -209,7 +217,7 @@ __device__ __forceinline__ void tmem_ld_wait_regs(uint32_t (&r0)[32], uint32_t (
     for (int t = 0; t < 32; ++t) asm volatile("" : "+r"(r0[t]), "+r"(r1[t]));
 }
 
-// Columns at or beyond k (padding of the last chunk) never win.
+// Columns at or beyond k (padding) never win.
 __device__ __forceinline__ void mask_tail(uint32_t (&r)[32], int64_t j0, int64_t k) {
     if (j0 + 32 > k) {
 #pragma unroll
@@ -281,7 +289,7 @@ __host__ __device__ constexpr float norm_coef(int bf16, int part) {
     return bf16 ? -1.f : (part == 0 ? -1024.f : (part == 1 ? -1.f : -0x1p-10f));
 }
 
-template <int BF16, int NKB, int NCH>
+template <int BF16, int NKB, int NCH, bool MULTI>
 __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArgs a) {
     if (a.guard != nullptr && *reinterpret_cast<const volatile int *>(&a.guard->done)) return;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -304,7 +312,8 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
     volatile int *err = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t n = a.n, k = a.k;
+    // k: columns from this pass's first on (the padding beyond never wins)
+    const int64_t n = a.n, k = a.k - a.col0;
     const long long lim = a.wait_limit;
     const int64_t ntiles = ceil_div<int64_t>(n, kTileM);
     const uint32_t cbytes = (uint32_t)cimg_bytes(NKB, k_pad);
@@ -350,8 +359,16 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
         // ------------------------------ producer ------------------------------
         if (lane == 0) {
             mbar_arrive_expect_tx(cbar, cbytes);
-            for (uint32_t off = 0; off < cbytes; off += 32768u)
-                bulk_g2s(cimg_s + off, a.cimg + off, min(32768u, cbytes - off), cbar);
+            // rows col0 .. col0 + k_pad - 1 of every feature block and of the
+            // half-norm block of the global image
+            for (int kb = 0; kb <= NKB; ++kb) {
+                const uint32_t row = kb < NKB ? 128u : kNormRowBytes;
+                const uint32_t bytes = (uint32_t)k_pad * row;
+                const uint8_t *src = a.cimg + (size_t)kb * a.k_img * 128 + (size_t)a.col0 * row;
+                uint8_t *dst = cimg_s + (size_t)kb * k_pad * 128;
+                for (uint32_t off = 0; off < bytes; off += 32768u)
+                    bulk_g2s(dst + off, src + off, min(32768u, bytes - off), cbar);
+            }
             int s = 0;
             uint32_t ph = 0, issued = 0u, last_ph = 0u;
             for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -497,7 +514,10 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                 tmem_ld32(cb, ra);
                 tmem_ld32(cb + 32, rb);
                 tmem_ld_wait_regs(ra, rb);
-                if (c == NCH - 1) {
+                // padding columns (at or beyond k) never win; a pass's padding
+                // may span several chunks
+                const bool pad = MULTI ? (int64_t)(c + 1) * kChunkN > k : c == NCH - 1;
+                if (pad) {
                     mask_tail(ra, j0, k);
                     mask_tail(rb, j0 + 32, k);
                 }
@@ -518,7 +538,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                 tmem_ld_wait_regs(ra, rb);
                 tc_fence_before();
                 mbar_arrive(&tempty[b]);  // the accumulator may be overwritten now
-                if (c == NCH - 1) {
+                if (pad) {
                     mask_tail(ra, j0 + 64, k);
                     mask_tail(rb, j0 + 96, k);
                 }
@@ -577,7 +597,23 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                 loser_hot = true;
             }
             int code = -1;  // handoff to the update warps: >= 0 label, <= -2 recheck slot
-            if (i < n) {
+            if (MULTI && i < n) {
+                // column pass: the pass's best score and both halves' masks
+                // (single bits for a unique winner), decided by the combine
+                uint32_t *cw = reinterpret_cast<uint32_t *>(a.cand + i);
+                if (win) {
+                    cw[h] = hot1;
+                    cw[2 + h] = hot2;
+                    if (!loser_hot) {
+                        cw[h ^ 1] = 0u;
+                        cw[2 + (h ^ 1)] = 0u;
+                    }
+                    a.pmax[i] = fmaxf(Mh, Mo);
+                } else if (loser_hot) {
+                    cw[h] = hot1;
+                    cw[2 + h] = hot2;
+                }
+            } else if (i < n) {
                 uint32_t *cw = reinterpret_cast<uint32_t *>(a.cand + i);
                 if (win) {
                     if (!loser_hot && __popc(hot1) == 1 && __popc(hot2) == 1) {
@@ -619,7 +655,8 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
         // Uncertified rows are left to the recheck kernel.
         const int u = threadIdx.x - 32 * (2 + kEpiWarps);
         const int64_t d4 = a.d4;
-        const int64_t cstride = k_pad * d4 + k_pad;
+        const int64_t ks = MULTI ? a.k_img : k_pad;  // rows of the cluster sums (all columns)
+        const int64_t cstride = ks * d4 + ks;
         float *sums32 = a.sums32 + (int64_t)(blockIdx.x % (unsigned)a.n_copies) * cstride;
         double *acc64 = a.acc64 + (int64_t)(blockIdx.x % (unsigned)a.n_copies) * cstride;
         auto consume = [&](int code, const float4 (&xv)[16], float wv, int pass) {
@@ -636,7 +673,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                         atomicAdd(dst + 4 * g + 3, (double)__fmul_rn(xv[g].w, wv));
                     }
                 }
-                if (pass == 0) atomicAdd(acc64 + k_pad * d4 + code, (double)wv);
+                if (pass == 0) atomicAdd(acc64 + ks * d4 + code, (double)wv);
             } else {
                 float4 *dst = reinterpret_cast<float4 *>(sums32 + (int64_t)code * d4 + pass * 64);
 #pragma unroll
@@ -650,7 +687,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                         atomicAdd(dst + g, v);
                     }
                 }
-                if (pass == 0) atomicAdd(sums32 + k_pad * d4 + code, wv);
+                if (pass == 0) atomicAdd(sums32 + ks * d4 + code, wv);
             }
         };
         int tl = 0;
@@ -767,9 +804,8 @@ __global__ void __launch_bounds__(kXImageThreads) x_image_kernel(
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t i0 = tile * kTileM;
         if (rowmajor) {
-            const int fshift = (nkb == 2) ? 7 : 6;  // F = 64 nkb
             for (int e = threadIdx.x; e < F * kTileM; e += kXImageThreads) {
-                const int r = e >> fshift, f = e & (F - 1);
+                const int r = e / F, f = e - r * F;
                 const int64_t i = i0 + r;
                 xs[f * kXsPitch + r] = (f < d && i < n) ? X[i * d + f] : 0.f;
             }
@@ -851,22 +887,25 @@ __global__ void c_image_kernel(const float *C, const float *hn, int64_t d, int64
     const double s2 = (double)sigma * (double)sigma;
     const float lim = max16<BF16>();
     bool ovf = false;
-    // One thread per (centroid row j, 8-feature chunk): G = 8 nkb consecutive
-    // lanes hold one row (k_pad G is a multiple of 32, so every warp is either
-    // entirely inside the range or entirely past it).
-    const int G = 8 * nkb;
+    // One thread per (centroid row j, 8-feature chunk): G = 8 nkb rounded up
+    // to a power of two consecutive lanes hold one row, the ones past its 8 nkb
+    // chunks idle (k_pad G is a multiple of 32, so every warp is either
+    // entirely inside the range or entirely past it, and a row's lanes never
+    // straddle two warps).
+    const int G = (nkb <= 1) ? 8 : (nkb == 2 ? 16 : 32);
     const int64_t total = k_pad * G;
     for (int64_t tt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; tt < total;
          tt += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = tt / G;
         const int qc = (int)(tt % G), kb = qc >> 3, ch = qc & 7;
+        const bool lane_used = kb < nkb;
         const int64_t f0 = (int64_t)kb * 64 + ch * 8;
         double q2 = 0.0, qd = 0.0;
         float v[8], xr[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
             const int64_t f = f0 + e;
-            const float x = (j < k && f < d) ? C[f * k + j] : 0.f;
+            const float x = (lane_used && j < k && f < d) ? C[f * k + j] : 0.f;
             q2 += (double)x * (double)x;
             float sv = x * sigma;
             if (!(fabsf(sv) <= lim)) {
@@ -878,17 +917,19 @@ __global__ void c_image_kernel(const float *C, const float *hn, int64_t d, int64
             v[e] = sv;
             xr[e] = x;
         }
-        // d4 is a multiple of 4 and f0 of 8: whole float4 stores
-        float4 *cdst = reinterpret_cast<float4 *>(ct + j * d4 + f0);
-        if (f0 < d4) cdst[0] = make_float4(xr[0], xr[1], xr[2], xr[3]);
-        if (f0 + 4 < d4) cdst[1] = make_float4(xr[4], xr[5], xr[6], xr[7]);
-        uint4 pk;
-        pk.x = pack2<BF16>(v[0], v[1]);
-        pk.y = pack2<BF16>(v[2], v[3]);
-        pk.z = pack2<BF16>(v[4], v[5]);
-        pk.w = pack2<BF16>(v[6], v[7]);
-        *reinterpret_cast<uint4 *>(img + (size_t)kb * k_pad * 128 +
-                                   sw128_offset((uint32_t)j, (uint32_t)ch * 8)) = pk;
+        if (lane_used) {
+            // d4 is a multiple of 4 and f0 of 8: whole float4 stores
+            float4 *cdst = reinterpret_cast<float4 *>(ct + j * d4 + f0);
+            if (f0 < d4) cdst[0] = make_float4(xr[0], xr[1], xr[2], xr[3]);
+            if (f0 + 4 < d4) cdst[1] = make_float4(xr[4], xr[5], xr[6], xr[7]);
+            uint4 pk;
+            pk.x = pack2<BF16>(v[0], v[1]);
+            pk.y = pack2<BF16>(v[2], v[3]);
+            pk.z = pack2<BF16>(v[4], v[5]);
+            pk.w = pack2<BF16>(v[6], v[7]);
+            *reinterpret_cast<uint4 *>(img + (size_t)kb * k_pad * 128 +
+                                       sw128_offset((uint32_t)j, (uint32_t)ch * 8)) = pk;
+        }
         // the row's squared norms over its G chunk lanes
         for (int o = G >> 1; o > 0; o >>= 1) {
             q2 += __shfl_xor_sync(0xffffffffu, q2, o);
@@ -994,11 +1035,18 @@ __device__ __forceinline__ uint32_t order_key(float v) {
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
+// Candidates of a flagged sample: per column pass p (cand[p * n + i], columns
+// offset by p * pass_cols; one pass unless n_clusters needed several), hot
+// sub-chunks x hot classes of each column half.
+__device__ __forceinline__ int pass_count(const uint4 &m) {
+    return __popc(m.x) * __popc(m.z) + __popc(m.y) * __popc(m.w);
+}
+
 __global__ void __launch_bounds__(kRecheckThreads) recheck_kernel(
     const float *xrow, const float *ct, const float *hn, const float *w, const uint4 *cand,
     const int *flagged, const int *n_flagged, int64_t n, int64_t d, int64_t k, int64_t d4,
     void *labels, int label64, int update, int acc_f64, float *sums32, double *acc64,
-    int64_t k_pad, int n_copies, const LoopState *guard) {
+    int64_t k_pad, int n_copies, const LoopState *guard, int passes, int64_t pass_cols) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
     constexpr int kWarps = kRecheckThreads / 32;
     __shared__ unsigned long long key_s[kWarps][32];
@@ -1021,14 +1069,18 @@ __global__ void __launch_bounds__(kRecheckThreads) recheck_kernel(
         const int64_t e = base + lane;
         int64_t i = -1;
         uint4 cm = make_uint4(0u, 0u, 0u, 0u);
+        int cnt = 0;
         if (e < total) {
             i = flagged[e];
-            if (i >= 0 && i < n) cm = cand[i];
-            else i = -1;
+            if (i >= 0 && i < n) {
+                cm = cand[i];
+                cnt = pass_count(cm);
+                for (int p = 1; p < passes; ++p) cnt += pass_count(cand[(int64_t)p * n + i]);
+            } else {
+                i = -1;
+            }
         }
         // candidates of this lane's sample: per column half, hot sub-chunks x hot classes
-        const int c0 = __popc(cm.x) * __popc(cm.z);
-        const int cnt = c0 + __popc(cm.y) * __popc(cm.w);
         int incl = cnt;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -1050,7 +1102,14 @@ __global__ void __launch_bounds__(kRecheckThreads) recheck_kernel(
             }
             const int owner = lo;
             int r = pr - (owner ? incl_s[wq][owner - 1] : 0);
-            const uint4 om = cm_s[wq][owner];
+            const int64_t oi = row_s[wq][owner];
+            uint4 om = cm_s[wq][owner];
+            int64_t jbase = 0;
+            for (int p = 1; p < passes && r >= pass_count(om); ++p) {
+                r -= pass_count(om);
+                om = cand[(int64_t)p * n + oi];
+                jbase += pass_cols;
+            }
             const int oc0 = __popc(om.x) * __popc(om.z);
             int h = 0;
             uint32_t m1 = om.x, m2 = om.z;
@@ -1065,9 +1124,8 @@ __global__ void __launch_bounds__(kRecheckThreads) recheck_kernel(
             for (int q = r / n2; q > 0; --q) m1 &= m1 - 1u;
             for (int q = r % n2; q > 0; --q) m2 &= m2 - 1u;
             const int sc = __ffs(m1) - 1, t = __ffs(m2) - 1;
-            const int64_t j = (int64_t)(sc >> 2) * kChunkN + h * 128 + (sc & 3) * 32 + t;
+            const int64_t j = jbase + (int64_t)(sc >> 2) * kChunkN + h * 128 + (sc & 3) * 32 + t;
             if (j >= k) continue;
-            const int64_t oi = row_s[wq][owner];
             const float4 *xr = reinterpret_cast<const float4 *>(xrow + oi * d4);
             const float4 *cr = reinterpret_cast<const float4 *>(ct + j * d4);
             float dot = 0.f;
@@ -1118,6 +1176,102 @@ __global__ void __launch_bounds__(kRecheckThreads) recheck_kernel(
             }
         }
         __syncwarp();  // this batch's keys and masks are read before the next batch
+    }
+}
+
+// After the column passes of one assignment: per sample the best score M
+// over the passes and thr = M - E2 (the bound the passes used).  Every
+// score within E2 / 2 of its exact value, a pass whose best score is below
+// thr holds no candidate; the pass masks were made against the pass's own
+// best score minus E2, which is at most thr, so a hot pass's masks hold a
+// superset of its candidates.  The sample is certified when exactly one pass
+// reaches thr and that pass has a unique winner (single bits in one half,
+// nothing in the other): its label is written and w x added to its cluster's
+// sums.  Otherwise the masks of the passes below thr are cleared and the
+// sample goes to the recheck list.
+__global__ void __launch_bounds__(256) combine_kernel(
+    const float *pmax, uint4 *cand, int passes, int64_t pass_cols, const float *nx,
+    const float *ndx, const MixedConsts *consts, const float *xrow, const float *w, void *labels,
+    int label64, int update, int acc_f64, float *sums32, double *acc64, int64_t k_pad,
+    int64_t d4, int n_copies, int *flagged, int *n_flagged, int64_t n, int64_t k,
+    const LoopState *guard) {
+    if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
+    const MixedConsts cst = *consts;
+    {
+        const int64_t copy = (int64_t)(blockIdx.x % (unsigned)n_copies) * (k_pad * d4 + k_pad);
+        sums32 += copy;
+        acc64 += copy;
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float e = fmaf(nx[i], cst.alpha, fmaf(ndx[i], cst.beta1, cst.beta0));
+        const float E2 = 2.f * e * 1.000001f;
+        float M = -pos_inf<float>();
+        bool nan = false;
+        for (int p = 0; p < passes; ++p) {
+            const float v = pmax[(int64_t)p * n + i];
+            nan |= !(v == v);
+            M = fmaxf(M, v);
+        }
+        const float thr = M - E2;
+        nan |= !(thr == thr);
+        int hot = 0, ph = -1;
+        for (int p = 0; p < passes; ++p)
+            if (nan || pmax[(int64_t)p * n + i] >= thr) {
+                ++hot;
+                ph = p;
+            }
+        int64_t label = -1;
+        if (!nan && hot == 1) {
+            const uint4 m = cand[(int64_t)ph * n + i];
+            const bool a0 = (m.x | m.z) != 0u, a1 = (m.y | m.w) != 0u;
+            if (a0 != a1) {
+                const int h = a1 ? 1 : 0;
+                const uint32_t h1 = h ? m.y : m.x, h2 = h ? m.w : m.z;
+                if (__popc(h1) == 1 && __popc(h2) == 1) {
+                    const int sc = __ffs(h1) - 1, t = __ffs(h2) - 1;
+                    label = (int64_t)ph * pass_cols + (int64_t)(sc >> 2) * kChunkN + h * 128 +
+                            (sc & 3) * 32 + t;
+                    if (label >= k) label = -1;
+                }
+            }
+        }
+        if (label >= 0) {
+            if (label64)
+                reinterpret_cast<int64_t *>(labels)[i] = label;
+            else
+                reinterpret_cast<int32_t *>(labels)[i] = (int32_t)label;
+            if (update) {
+                const float4 *xr = reinterpret_cast<const float4 *>(xrow + i * d4);
+                const float wv = w[i];
+                if (acc_f64) {
+                    double *dst = acc64 + label * d4;
+                    for (int64_t g = 0; g < d4 / 4; ++g) {
+                        const float4 xv = __ldg(xr + g);
+                        atomicAdd(dst + 4 * g + 0, (double)__fmul_rn(xv.x, wv));
+                        atomicAdd(dst + 4 * g + 1, (double)__fmul_rn(xv.y, wv));
+                        atomicAdd(dst + 4 * g + 2, (double)__fmul_rn(xv.z, wv));
+                        atomicAdd(dst + 4 * g + 3, (double)__fmul_rn(xv.w, wv));
+                    }
+                    atomicAdd(acc64 + k_pad * d4 + label, (double)wv);
+                } else {
+                    float4 *dst = reinterpret_cast<float4 *>(sums32 + label * d4);
+                    for (int64_t g = 0; g < d4 / 4; ++g) {
+                        const float4 xv = __ldg(xr + g);
+                        atomicAdd(dst + g, make_float4(__fmul_rn(xv.x, wv), __fmul_rn(xv.y, wv),
+                                                       __fmul_rn(xv.z, wv), __fmul_rn(xv.w, wv)));
+                    }
+                    atomicAdd(sums32 + k_pad * d4 + label, wv);
+                }
+            }
+        } else {
+            if (!nan)
+                for (int p = 0; p < passes; ++p)
+                    if (!(pmax[(int64_t)p * n + i] >= thr))
+                        cand[(int64_t)p * n + i] = make_uint4(0u, 0u, 0u, 0u);
+            const int pos = atomicAdd(n_flagged, 1);
+            if (pos >= 0 && pos < n) flagged[pos] = (int)i;
+        }
     }
 }
 
@@ -1177,23 +1331,54 @@ __global__ void stats_kernel(const int *n_flagged, long long *last, long long *t
 
 using MixedKernel = void (*)(MixedArgs);
 
+// The widest pass each feature-block count takes (shared memory); column
+// passes always use it, so only those shapes have a multi-pass kernel.
+constexpr int max_chunks(int nkb) { return nkb == 1 ? 4 : (nkb == 2 ? 2 : 1); }
+
 template <int BF16, int NKB>
-MixedKernel pick_chunks(int nch) {
+MixedKernel pick_chunks(int nch, bool multi) {
+    constexpr int W = max_chunks(NKB);
+    if (multi) return nch == W ? mixed_assign_kernel<BF16, NKB, W, true> : nullptr;
     switch (nch) {
-        case 1: return mixed_assign_kernel<BF16, NKB, 1>;
-        case 2: return mixed_assign_kernel<BF16, NKB, 2>;
-        case 3: return NKB == 1 ? mixed_assign_kernel<BF16, 1, 3> : nullptr;
-        case 4: return NKB == 1 ? mixed_assign_kernel<BF16, 1, 4> : nullptr;
+        case 1: return mixed_assign_kernel<BF16, NKB, 1, false>;
+        case 2: return W >= 2 ? mixed_assign_kernel<BF16, NKB, (W >= 2 ? 2 : 1), false> : nullptr;
+        case 3: return W >= 3 ? mixed_assign_kernel<BF16, NKB, (W >= 3 ? 3 : 1), false> : nullptr;
+        case 4: return W >= 4 ? mixed_assign_kernel<BF16, NKB, (W >= 4 ? 4 : 1), false> : nullptr;
         default: return nullptr;
     }
 }
 
-// Kernel for (operand type, 64-feature blocks, 256-column chunks).  Two
-// feature blocks leave shared memory for at most two chunks.
-MixedKernel pick_kernel(int bf16, int nkb, int nch) {
-    if (nkb == 1) return bf16 ? pick_chunks<1, 1>(nch) : pick_chunks<0, 1>(nch);
-    if (nkb == 2) return bf16 ? pick_chunks<1, 2>(nch) : pick_chunks<0, 2>(nch);
-    return nullptr;
+// Kernel for (operand type, 64-feature blocks, 256-column chunks per pass,
+// column passes or one).
+MixedKernel pick_kernel(int bf16, int nkb, int nch, bool multi = false) {
+    switch (nkb) {
+        case 1: return bf16 ? pick_chunks<1, 1>(nch, multi) : pick_chunks<0, 1>(nch, multi);
+        case 2: return bf16 ? pick_chunks<1, 2>(nch, multi) : pick_chunks<0, 2>(nch, multi);
+        case 3: return bf16 ? pick_chunks<1, 3>(nch, multi) : pick_chunks<0, 3>(nch, multi);
+        case 4: return bf16 ? pick_chunks<1, 4>(nch, multi) : pick_chunks<0, 4>(nch, multi);
+        default: return nullptr;
+    }
+}
+
+// Up to 4 feature blocks (d <= 256) fit next to one 256-column chunk.
+constexpr int kMaxFeatureBlocks = 4;
+
+// Column chunks per pass and X-ring depth for nkb feature blocks: the widest
+// pass (at most kMaxChunks chunks, and no wider than needed for kp columns)
+// that fits shared memory with a ring of at least two stages, else one stage.
+bool pass_plan(int nkb, int64_t kp, int64_t d4, int *nch_out, int *stages_out) {
+    const int want = (int)std::min<int64_t>(max_chunks(nkb), kp / kChunkN);
+    for (int nch = want; nch >= 1; --nch) {
+        if (pick_kernel(0, nkb, nch) == nullptr) continue;
+        for (int st = 4; st >= 1; --st)
+            if (smem_layout(nkb, (int64_t)nch * kChunkN, d4, st).total <= kSmemLimit) {
+                if (st == 1 && nch > 1) break;  // a narrower pass keeps a two-stage ring
+                *nch_out = nch;
+                *stages_out = st;
+                return true;
+            }
+    }
+    return false;
 }
 
 unsigned grid1d(int64_t work, int block, int cap = 8192) {
@@ -1242,12 +1427,17 @@ struct MixedFit : PlainFit<float, I> {
         *ss = d4;
     }
 
+    int nch = 1;     // 256-column chunks per pass
+    int passes = 1;  // column passes per assignment (n_clusters beyond one pass)
+    float *pmax = nullptr;
+
     static bool supported(int64_t d, int64_t k) {
         const int nk = (int)ceil_div<int64_t>(std::max<int64_t>(d, 1), 64);
-        const int64_t kp = ceil_div<int64_t>(std::max<int64_t>(k, 1), kChunkN) * kChunkN;
-        if (nk > 2 || kp > (int64_t)kMaxChunks * kChunkN) return false;
+        if (nk > kMaxFeatureBlocks || k < 1) return false;
+        const int64_t kp = ceil_div<int64_t>(k, kChunkN) * kChunkN;
         const int64_t dd = ceil_div<int64_t>(std::max<int64_t>(d, 1), 4) * 4;
-        return smem_layout(nk, kp, dd, 2).total <= kSmemLimit;
+        int c = 0, st = 0;
+        return pass_plan(nk, kp, dd, &c, &st);
     }
 
     int init_mixed(int form) {
@@ -1255,24 +1445,19 @@ struct MixedFit : PlainFit<float, I> {
         cudaStream_t s = p.stream;
         bf16 = (form == KMC_FORM_MIXED_BF16) ? 1 : 0;
         nkb = (int)ceil_div<int64_t>(std::max<int64_t>(p.d, 1), 64);
-        k_pad = ceil_div<int64_t>(p.k, kChunkN) * kChunkN;
         d4 = ceil_div<int64_t>(std::max<int64_t>(p.d, 1), 4) * 4;
         ntiles = ceil_div<int64_t>(p.n, kTileM);
+        if (!pass_plan(nkb, ceil_div<int64_t>(p.k, kChunkN) * kChunkN, d4, &nch, &stages)) {
+            set_error("mixed form: operands do not fit in shared memory");
+            return KMC_ERR_UNSUPPORTED;
+        }
+        // the centroid image has whole passes of rows (zero padding)
+        passes = (int)ceil_div<int64_t>(p.k, (int64_t)nch * kChunkN);
+        k_pad = (int64_t)passes * nch * kChunkN;
         // Cluster sums: up to 32 features, float64 reductions per feature
         // (a few per sample; they keep the trajectory on the float64
         // reference's), beyond that float32 four-wide reductions.
         acc_f64 = d4 <= 32 ? 1 : 0;
-        // the deepest X ring that fits next to the centroid image
-        bool found = false;
-        for (int st = 4; st >= 2 && !found; --st)
-            if (smem_layout(nkb, k_pad, d4, st).total <= kSmemLimit) {
-                stages = st;
-                found = true;
-            }
-        if (!found) {
-            set_error("mixed form: operands do not fit in shared memory");
-            return KMC_ERR_UNSUPPORTED;
-        }
         size_t off = 0;
         auto take = [&](size_t bytes) {
             size_t o = off;
@@ -1301,7 +1486,9 @@ struct MixedFit : PlainFit<float, I> {
         const size_t o_cn2 = take(sizeof(float) * p.k);
         const size_t o_dcn = take(sizeof(float) * p.k);
         const size_t o_cst = take(sizeof(MixedConsts));
-        const size_t o_cand = take(sizeof(uint4) * p.n);
+        // candidate masks (and best scores) of every column pass
+        const size_t o_cand = take(sizeof(uint4) * (size_t)p.n * passes);
+        const size_t o_pmax = take(passes > 1 ? sizeof(float) * (size_t)p.n * passes : 16);
         const size_t o_flg = take(sizeof(int) * p.n);
         const size_t o_cnt = take(sizeof(int) * 4);
         const size_t o_st = take(sizeof(long long) * 2);
@@ -1319,6 +1506,7 @@ struct MixedFit : PlainFit<float, I> {
         dcn = reinterpret_cast<float *>(b + o_dcn);
         consts = reinterpret_cast<MixedConsts *>(b + o_cst);
         cand = reinterpret_cast<uint4 *>(b + o_cand);
+        pmax = reinterpret_cast<float *>(b + o_pmax);
         flagged = reinterpret_cast<int *>(b + o_flg);
         n_flagged = reinterpret_cast<int *>(b + o_cnt);
         err_dev = n_flagged + 1;
@@ -1350,11 +1538,12 @@ struct MixedFit : PlainFit<float, I> {
     int centroid_prep(const float *cur, const LoopState *guard) {
         const FitParams<float, I> &p = this->prm;
         cudaStream_t s = p.stream;
+        const int64_t lanes = k_pad * (nkb <= 1 ? 8 : (nkb == 2 ? 16 : 32));  // c_image's G
         if (bf16)
-            c_image_kernel<1><<<grid1d(k_pad * 8 * nkb, 128, 4096), 128, 0, s>>>(
+            c_image_kernel<1><<<grid1d(lanes, 128, 4096), 128, 0, s>>>(
                 cur, this->hn, p.d, p.k, k_pad, nkb, consts, cimg, cn2, dcn, ct, d4, guard);
         else
-            c_image_kernel<0><<<grid1d(k_pad * 8 * nkb, 128, 4096), 128, 0, s>>>(
+            c_image_kernel<0><<<grid1d(lanes, 128, 4096), 128, 0, s>>>(
                 cur, this->hn, p.d, p.k, k_pad, nkb, consts, cimg, cn2, dcn, ct, d4, guard);
         KMC_TRY(check_launch("c_image"));
         bound_kernel<<<1, 1024, 0, s>>>(cn2, dcn, this->hn, p.d, p.k, bf16, consts, guard);
@@ -1400,19 +1589,36 @@ struct MixedFit : PlainFit<float, I> {
         a.stall = stall_once;
         a.state = this->state;
         stall_once = 0;
-        const SmemLayout L = smem_layout(nkb, k_pad, d4, stages);
-        auto kern = pick_kernel(bf16, nkb, (int)(k_pad / kChunkN));
+        const int64_t pass_cols = (int64_t)nch * kChunkN;
+        a.k_pad = pass_cols;
+        a.k_img = k_pad;
+        a.multi = passes > 1 ? 1 : 0;
+        if (a.multi) a.update = 0;  // the combine accumulates the certified samples
+        const SmemLayout L = smem_layout(nkb, pass_cols, d4, stages);
+        auto kern = pick_kernel(bf16, nkb, nch, a.multi != 0);
         if (kern == nullptr) {
-            set_error("mixed form: no kernel for %d feature blocks and %lld chunks", nkb,
-                      (long long)(k_pad / kChunkN));
+            set_error("mixed form: no kernel for %d feature blocks and %d chunks", nkb, nch);
             return KMC_ERR_UNSUPPORTED;
         }
         KMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)L.total));
         const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(ntiles, num_sms()));
         if (p.n > 0) {
-            kern<<<(unsigned)grid, kThreadsMixed, L.total, s>>>(a);
-            KMC_TRY(check_launch("mixed_assign"));
+            for (int ps = 0; ps < passes; ++ps) {
+                a.col0 = (int64_t)ps * pass_cols;
+                a.cand = cand + (int64_t)ps * p.n;
+                a.pmax = pmax + (a.multi ? (int64_t)ps * p.n : 0);
+                kern<<<(unsigned)grid, kThreadsMixed, L.total, s>>>(a);
+                KMC_TRY(check_launch("mixed_assign"));
+                a.stall = 0;
+            }
+            if (a.multi) {
+                combine_kernel<<<grid1d(p.n, 256, num_sms() * 8), 256, 0, s>>>(
+                    pmax, cand, passes, pass_cols, nx, ndx, consts, xrow, p.w, p.labels, a.label64,
+                    update, acc_f64, sums32, acc64, k_pad, d4, n_copies, flagged, n_flagged, p.n,
+                    p.k, guard);
+                KMC_TRY(check_launch("mixed_combine"));
+            }
         }
         // enough CTAs for every sample flagged (8 warps of 32 per CTA round),
         // at most 8 per SM
@@ -1420,14 +1626,14 @@ struct MixedFit : PlainFit<float, I> {
             1, std::min<int64_t>((int64_t)num_sms() * 8, ceil_div<int64_t>(p.n, kRecheckThreads)));
         recheck_kernel<<<(unsigned)rgrid, kRecheckThreads, 0, s>>>(
             xrow, ct, this->hn, p.w, cand, flagged, n_flagged, p.n, p.d, p.k, d4, p.labels,
-            a.label64, update, acc_f64, sums32, acc64, k_pad, n_copies, guard);
+            a.label64, update, acc_f64, sums32, acc64, k_pad, n_copies, guard, passes, pass_cols);
         KMC_TRY(check_launch("mixed_recheck"));
         stats_kernel<<<1, 1, 0, s>>>(n_flagged, stats, stats + 1, guard);
         return check_launch("mixed_stats");
     }
 
     int step_assign_and_accumulate(const float *cur, int64_t *n_launches) override {
-        *n_launches = 6;
+        *n_launches = 6 + (passes > 1 ? passes : 0);
         return assign_pass(cur, 1, this->state);
     }
 
@@ -1469,9 +1675,8 @@ int make_mixed_fit(const FitParams<T, I> &p, int form, std::unique_ptr<FitBase> 
         return KMC_ERR_UNSUPPORTED;
     } else {
         if (!MixedFit<I>::supported(p.d, p.k)) {
-            set_error("mixed form supports n_features <= 128 and n_clusters <= %d within %zu "
-                      "bytes of shared memory (got d=%lld, k=%lld)",
-                      kMaxChunks * kChunkN, kSmemLimit, (long long)p.d, (long long)p.k);
+            set_error("mixed form supports n_features <= %d (got d=%lld, k=%lld)",
+                      64 * kMaxFeatureBlocks, (long long)p.d, (long long)p.k);
             return KMC_ERR_UNSUPPORTED;
         }
         auto f = std::make_unique<MixedFit<I>>();

@@ -49,7 +49,10 @@ def _fit_labels(X, C0, form, max_iter=0, tol=0.0):
 
 
 SHAPES = [(300, 64, 256), (1000, 3, 8), (5000, 14, 127), (20000, 64, 1024), (7777, 100, 300),
-          (4096, 33, 511), (129, 128, 512), (20000, 16, 1024), (3001, 65, 257)]
+          (4096, 33, 511), (129, 128, 512), (20000, 16, 1024), (3001, 65, 257),
+          # several column passes (k beyond one launch) and 3-4 feature blocks
+          (20000, 64, 2048), (5000, 64, 1025), (3000, 100, 513), (4000, 200, 300), (3000, 129, 64),
+          (2000, 256, 100), (6000, 20, 3000), (2500, 180, 700)]
 
 
 @pytest.mark.parametrize("n,d,k", SHAPES)
@@ -65,8 +68,8 @@ def test_mixed_assignment_equals_reference_labels(oracle, n, d, k, form):
     assert 0 <= last <= n
 
 
-@pytest.mark.parametrize("d,k", [(64, 1025), (129, 64), (100, 513)])
-def test_mixed_rejects_unsupported_shapes(d, k):
+@pytest.mark.parametrize("d,k", [(257, 64), (300, 8)])
+def test_mixed_rejects_more_than_256_features(d, k):
     X = np.zeros((d, 256), np.float32)
     C = np.zeros((d, k), np.float32)
     with pytest.raises(RuntimeError, match="kmc error 4"):
@@ -100,6 +103,8 @@ def _near_tie_mask(X, C, rel=1e-5):
 # are chosen by the squared distances the assignment pass writes.
 @pytest.mark.parametrize("case", [("c1_50k_d14_k16", 50_000, 14, 16, 16, (-10, 10), 1.0, 0, 1e-4, 100),
                                   ("d32_k200", 40_000, 32, 100, 200, (-5, 5), 1.0, 3, 0.0, 10),
+                                  ("d16_k1500_passes", 60_000, 16, 700, 1500, (-10, 10), 1.0, 5, 0.0,
+                                   6),
                                   ("d14_k127_forced_empty", 100_000, 14, 127, 127, (-10, 10), 1.5, 1,
                                    0.0, 8, True)])
 @pytest.mark.parametrize("form", sorted(FORMS))
@@ -128,7 +133,10 @@ def test_mixed_driver_tracks_oracle(oracle, case, form):
                                   ("d64_k1024_sigma", 100_000, 64, 1024, 1024, (-5, 5), (0.5, 2.0), 2, 4),
                                   ("d100_k300", 30_000, 100, 150, 300, (-5, 5), 1.0, 4, 3),
                                   ("d64_k256_forced_empty", 60_000, 64, 256, 256, (-5, 5), 1.0, 6, 3,
-                                   True)])
+                                   True),
+                                  ("d64_k2048_passes", 60_000, 64, 1500, 2048, (-5, 5), 1.0, 7, 3),
+                                  ("d200_k600_passes_forced_empty", 20_000, 200, 300, 600, (-5, 5),
+                                   1.0, 8, 3, True)])
 @pytest.mark.parametrize("form", sorted(FORMS))
 def test_mixed_iterations_match_oracle_step_by_step(oracle, case, form):
     import torch
