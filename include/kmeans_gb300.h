@@ -499,6 +499,19 @@ int kmc_fit_rechecked(kmc_fit_t fit, int64_t *last_out, int64_t *total_out, int 
  * after `clocks`: a test of the timeout path that faults and hangs nothing.
  * The plain form has no device-side waits and ignores both. */
 int kmc_fit_set_wait_limit(kmc_fit_t fit, int64_t clocks, int stall_once);
+/* No counterpart in the reference (whose kernels take a window height and a
+ * work-group size as arguments).  The plain form's kernels choose their
+ * centroid-tile width themselves: the first fit of a (n_features, power-of-two
+ * bucket of n_clusters, dtype) times each width (128 / 64 / 32 centroids for
+ * float32, 64 / 32 for float64) on a synthetic instance and caches the fastest
+ * in memory and in $KMC_TILE_CACHE (default $XDG_CACHE_HOME or ~/.cache,
+ * kmeans_gb300/tiles.txt); KMC_TUNE=0 turns the search off.  Every width gives
+ * the same labels.  kmc_fit_tile_variant returns (tuning if needed) the choice
+ * (0, 1, 2) for dtype_bytes 4 or 8; kmc_fit_set_tile_variant overrides a
+ * session's. */
+int kmc_fit_tile_variant(int64_t n_features, int64_t n_clusters, int dtype_bytes,
+                         kmc_stream_t stream, int *variant_out);
+int kmc_fit_set_tile_variant(kmc_fit_t fit, int variant);
 /* Kernel launches enqueued so far by this session. */
 int kmc_fit_launch_count(kmc_fit_t fit, int64_t *launches_out);
 int kmc_fit_destroy(kmc_fit_t fit);

@@ -25,6 +25,7 @@
 #include <cstdlib>
 #include <fstream>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <sstream>
 #include <string>
@@ -479,7 +480,9 @@ int launch_assign_v(int variant, const BInst *tab, const BItem *items, int n_ite
 }
 
 std::mutex g_tune_mu;
-std::map<std::pair<int64_t, int64_t>, int> g_tune;
+// autotuner choices by (d, power-of-two bucket of k, tag); tag "f32" is the
+// batched engine's centroid window, "fit-f32" / "fit-f64" the single-fit tile
+std::map<std::tuple<int64_t, int64_t, std::string>, int> g_tune;
 bool g_tune_loaded = false;
 
 std::string tune_path() {
@@ -494,6 +497,7 @@ std::string tune_path() {
     return base + "/kmeans_gb300/tiles.txt";
 }
 
+// Lines "d k tag variant"; later lines win.
 void tune_load() {
     const std::string p = tune_path();
     if (p.empty()) return;
@@ -502,14 +506,13 @@ void tune_load() {
     while (std::getline(f, line)) {
         std::istringstream is(line);
         int64_t d = 0, k = 0;
-        std::string dt;
+        std::string tag;
         int v = -1;
-        if (is >> d >> k >> dt >> v && dt == "f32" && v >= 0 && v < kBatchVariants)
-            g_tune[{d, k}] = v;
+        if (is >> d >> k >> tag >> v && v >= 0 && v < 8) g_tune[{d, k, tag}] = v;
     }
 }
 
-void tune_store(int64_t d, int64_t k, int v) {
+void tune_store(int64_t d, int64_t k, const std::string &tag, int v) {
     const std::string p = tune_path();
     if (p.empty()) return;
     const size_t slash = p.rfind('/');
@@ -521,7 +524,7 @@ void tune_store(int64_t d, int64_t k, int v) {
         mkdir(dir.c_str(), 0755);
     }
     std::ofstream f(p, std::ios::app);
-    if (f) f << d << " " << k << " f32 " << v << "\n";
+    if (f) f << d << " " << k << " " << tag << " " << v << "\n";
 }
 
 }  // namespace
@@ -615,20 +618,29 @@ void seeded_rows(int64_t n, int64_t k, uint64_t seed, std::vector<int32_t> *out)
         (*out)[(size_t)j] = (int32_t)((a % (uint64_t)n * (uint64_t)j + b) % (uint64_t)n);
 }
 
-int tune_variant(int64_t d, int64_t k_in, cudaStream_t s, int *variant) {
-    // one measurement per (d, power-of-two bucket of k)
-    int64_t k = 1;
-    while (k < k_in) k <<= 1;
+bool tune_lookup(int64_t d, int64_t k, const char *tag, int *v) {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     if (!g_tune_loaded) {
         tune_load();
         g_tune_loaded = true;
     }
-    auto it = g_tune.find({d, k});
-    if (it != g_tune.end()) {
-        *variant = it->second;
-        return KMC_OK;
-    }
+    auto it = g_tune.find({d, k, std::string(tag)});
+    if (it == g_tune.end()) return false;
+    *v = it->second;
+    return true;
+}
+
+void tune_record(int64_t d, int64_t k, const char *tag, int v) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune[{d, k, std::string(tag)}] = v;
+    tune_store(d, k, tag, v);
+}
+
+int tune_variant(int64_t d, int64_t k_in, cudaStream_t s, int *variant) {
+    // one measurement per (d, power-of-two bucket of k)
+    int64_t k = 1;
+    while (k < k_in) k <<= 1;
+    if (tune_lookup(d, k, "f32", variant) && *variant < kBatchVariants) return KMC_OK;
     // Time the three assign kernels on a synthetic fitting instance of this
     // (d, k): 256 tiles of 128 samples, blobs around k centres.
     const int64_t n = 256 * kBatchTileM;
@@ -694,8 +706,7 @@ int tune_variant(int64_t d, int64_t k_in, cudaStream_t s, int *variant) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     KMC_CUDA_TRY(cudaStreamSynchronize(s));
-    g_tune[{d, k}] = best;
-    tune_store(d, k, best);
+    tune_record(d, k, "f32", best);
     *variant = best;
     return KMC_OK;
 }

@@ -488,6 +488,19 @@ int kmc_fit_set_wait_limit(kmc_fit_t fit, int64_t clocks, int stall_once) {
     KMC_FIT_CHECK(fit);
     return fit->impl->set_wait_limit((long long)clocks, stall_once);
 }
+int kmc_fit_set_tile_variant(kmc_fit_t fit, int variant) {
+    KMC_FIT_CHECK(fit);
+    return fit->impl->set_tile_variant(variant);
+}
+int kmc_fit_tile_variant(int64_t n_features, int64_t n_clusters, int dtype_bytes,
+                         kmc_stream_t stream, int *variant_out) {
+    KMC_CHECK_ARG(variant_out != nullptr, "null output");
+    KMC_CHECK_ARG(dtype_bytes == 4 || dtype_bytes == 8, "dtype_bytes must be 4 or 8");
+    KMC_CHECK_ARG(n_features >= 1 && n_clusters >= 1, "invalid sizes");
+    if (dtype_bytes == 4) return kmc::tune_fit_variant<float>(n_features, n_clusters, S(stream),
+                                                              variant_out);
+    return kmc::tune_fit_variant<double>(n_features, n_clusters, S(stream), variant_out);
+}
 int kmc_fit_launch_count(kmc_fit_t fit, int64_t *out) {
     KMC_FIT_CHECK(fit);
     KMC_CHECK_ARG(out != nullptr, "null output pointer");

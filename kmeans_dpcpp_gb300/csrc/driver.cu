@@ -68,6 +68,8 @@ int PlainFit<T, I>::init(const FitParams<T, I> &p) {
     const size_t o_tsc = take(threshold_scratch_bytes());
     const size_t o_ssc = take(select_scratch_bytes(k));
     KMC_TRY(ws.alloc(off, p.stream));
+    // the plain kernels' centroid-tile width for this (d, k, dtype)
+    if (uses_private_copies()) KMC_TRY(tune_fit_variant<T>(d, k, p.stream, &tile_variant));
     if (p.x_rowmajor && !reads_rowmajor()) {
         KMC_TRY(xt.alloc(sizeof(T) * (size_t)n * (size_t)d, p.stream));
         if (sizeof(T) == 4)
@@ -182,7 +184,7 @@ int PlainFit<T, I>::step_assign_and_accumulate(const T *cur, int64_t *n_launches
     const FitParams<T, I> &p = prm;
     *n_launches = 1;
     return launch_fused_step<T, I, double>(p.X, p.w, cur, hn, p.labels, sums_cp, sizes_cp, p.n,
-                                           p.d, p.k, P, p.stream, state);
+                                           p.d, p.k, P, p.stream, state, tile_variant);
 }
 
 template <typename T, typename I>
@@ -266,7 +268,8 @@ int PlainFit<T, I>::reduce_step(T *nxt) {
 template <typename T, typename I>
 int PlainFit<T, I>::final_assignment() {
     const FitParams<T, I> &p = prm;
-    return launch_assignment<T, I>(p.X, p.centroids, hn, p.labels, p.n, p.d, p.k, p.stream);
+    return launch_assignment<T, I>(p.X, p.centroids, hn, p.labels, p.n, p.d, p.k, p.stream,
+                                   nullptr, tile_variant);
 }
 
 template struct PlainFit<float, int32_t>;

@@ -31,12 +31,19 @@
 // for bit, so a zero tolerance stops it on the same iteration as a sequential
 // implementation (atomics in arbitrary order leave last-bit noise in every
 // centroid shift).
+#include <cstdlib>
+#include <type_traits>
+
 #include "km_kernels.cuh"
 
 namespace kmc {
 
 namespace {
 
+// Register micro-tile TM x TN per thread (BM = 16 TM samples x BN = 16 TN
+// centroids per CTA tile).  TN is a template argument of the kernels: the
+// autotuner picks the centroid-tile width per (d, k, dtype) (narrower tiles
+// waste fewer padded columns when k is small); TileCfg holds the default.
 template <typename T>
 struct TileCfg;
 template <>
@@ -47,6 +54,12 @@ template <>
 struct TileCfg<double> {
     static constexpr int TM = 4, TN = 4, BK = 16;
 };
+
+// Micro-tile width of autotuner variant v (0 = TileCfg's, then halves).
+template <typename T>
+__host__ __device__ constexpr int variant_tn(int v) {
+    return v <= 0 ? TileCfg<T>::TN : (v == 1 ? TileCfg<T>::TN / 2 : 2);
+}
 
 constexpr int kThreads = 256;
 constexpr int MODE_ASSIGN = 0, MODE_FUSED = 1, MODE_DIST = 2;
@@ -85,25 +98,40 @@ struct VecLd<float, 4> {
     }
 };
 template <>
+struct VecLd<float, 2> {
+    __device__ static void ld(const float *p, float *o) {
+        float2 v = *reinterpret_cast<const float2 *>(p);
+        o[0] = v.x; o[1] = v.y;
+    }
+};
+template <>
+struct VecLd<float, 1> {
+    __device__ static void ld(const float *p, float *o) { o[0] = *p; }
+};
+template <>
 struct VecLd<double, 2> {
     __device__ static void ld(const double *p, double *o) {
         double2 v = *reinterpret_cast<const double2 *>(p);
         o[0] = v.x; o[1] = v.y;
     }
 };
+template <>
+struct VecLd<double, 1> {
+    __device__ static void ld(const double *p, double *o) { o[0] = *p; }
+};
 
-template <typename T>
+template <typename T, int TN_ = TileCfg<T>::TN>
 struct TileSmem {
-    static constexpr int TM = TileCfg<T>::TM, TN = TileCfg<T>::TN, BK = TileCfg<T>::BK;
+    static constexpr int TM = TileCfg<T>::TM, TN = TN_, BK = TileCfg<T>::BK;
     static constexpr int BM = 16 * TM, BN = 16 * TN;
     static constexpr size_t base_bytes =
         sizeof(T) * (2 * BK * BM + 2 * BK * BN + BN + BM) + sizeof(long long) * BM;
 };
 
-template <typename T, typename I, int MODE, typename A>
+template <typename T, typename I, int MODE, typename A, int TN>
 __global__ void __launch_bounds__(kThreads, 2) tile_kernel(TileArgs<T, I, A> a) {
     if (a.guard != nullptr && *reinterpret_cast<const volatile int *>(&a.guard->done)) return;
-    constexpr int TM = TileCfg<T>::TM, TN = TileCfg<T>::TN, BK = TileCfg<T>::BK;
+    constexpr int TM = TileCfg<T>::TM, BK = TileCfg<T>::BK;
     constexpr int BM = 16 * TM, BN = 16 * TN;
     constexpr int HM = TM / 2, HN = TN / 2;
     constexpr int XR = BK * BM / kThreads, CR = BK * BN / kThreads;
@@ -343,12 +371,12 @@ __global__ void __launch_bounds__(kThreads, 2) tile_kernel(TileArgs<T, I, A> a) 
     }
 }
 
-template <typename T, typename I, int MODE, typename A = T>
+template <typename T, typename I, int MODE, typename A = T, int TN = TileCfg<T>::TN>
 int launch_tile(TileArgs<T, I, A> args, cudaStream_t s) {
     if (args.n == 0) return KMC_OK;
-    size_t smem = TileSmem<T>::base_bytes;
+    size_t smem = TileSmem<T, TN>::base_bytes;
     if (MODE == MODE_FUSED && args.priv) smem += sizeof(A) * (size_t)(args.d * args.k + args.k);
-    auto kern = tile_kernel<T, I, MODE, A>;
+    auto kern = tile_kernel<T, I, MODE, A, TN>;
     if (smem > 48 * 1024) {
         KMC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem));
@@ -356,7 +384,7 @@ int launch_tile(TileArgs<T, I, A> args, cudaStream_t s) {
     int per_sm = 0;
     KMC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
     if (per_sm < 1) per_sm = 1;
-    int64_t tiles = ceil_div<int64_t>(args.n, TileSmem<T>::BM);
+    int64_t tiles = ceil_div<int64_t>(args.n, TileSmem<T, TN>::BM);
     int64_t grid = (int64_t)num_sms() * per_sm;
     if (MODE == MODE_DIST) grid = tiles;  // output-bound: one tile per CTA
     if (grid > tiles) grid = tiles;
@@ -370,16 +398,18 @@ int launch_tile(TileArgs<T, I, A> args, cudaStream_t s) {
 
 template <typename T, typename I>
 int launch_assignment(const T *X, const T *C, const T *hn, I *labels, int64_t n, int64_t d,
-                      int64_t k, cudaStream_t s, const LoopState *guard) {
+                      int64_t k, cudaStream_t s, const LoopState *guard, int variant) {
     TileArgs<T, I> a{X, nullptr, C, hn, labels, nullptr, nullptr, nullptr, n, d, k, 1, 0, 0,
                      guard};
+    if (variant == 1) return launch_tile<T, I, MODE_ASSIGN, T, variant_tn<T>(1)>(a, s);
+    if (variant == 2) return launch_tile<T, I, MODE_ASSIGN, T, variant_tn<T>(2)>(a, s);
     return launch_tile<T, I, MODE_ASSIGN>(a, s);
 }
 
 template <typename T, typename I, typename A>
 int launch_fused_step(const T *X, const T *w, const T *C, const T *hn, I *labels, A *sums_cp,
                       A *sizes_cp, int64_t n, int64_t d, int64_t k, int64_t P, cudaStream_t s,
-                      const LoopState *guard) {
+                      const LoopState *guard, int variant) {
     // float64 sums of float samples with one copy per CTA go straight to
     // global memory (native reductions); otherwise small sums are privatised
     // in shared memory (float64 samples: ordered plain updates, no atomics)
@@ -387,6 +417,11 @@ int launch_fused_step(const T *X, const T *w, const T *C, const T *hn, I *labels
     int priv = (fits && (sizeof(T) == 8 || !(sizeof(A) == 8 && P > 1))) ? 1 : 0;
     TileArgs<T, I, A> a{X, w, C, hn, labels, sums_cp, sizes_cp, nullptr, n, d, k, P, priv, 0,
                         guard};
+    // the variants are instantiated for the driver's float64 sums
+    if constexpr (std::is_same<A, double>::value) {
+        if (variant == 1) return launch_tile<T, I, MODE_FUSED, A, variant_tn<T>(1)>(a, s);
+        if (variant == 2) return launch_tile<T, I, MODE_FUSED, A, variant_tn<T>(2)>(a, s);
+    }
     return launch_tile<T, I, MODE_FUSED, A>(a, s);
 }
 
@@ -398,24 +433,108 @@ int launch_distances(const T *X, const T *C, T *out, int64_t n, int64_t d, int64
     return launch_tile<T, int32_t, MODE_DIST>(a, s);
 }
 
+namespace {
+
+// Seeded uniform [-4, 4) samples for the autotuner's synthetic instance.
+template <typename T>
+__global__ void tune_fill_kernel(T *x, int64_t count, uint64_t seed) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t z = (uint64_t)e * 0x9E3779B97F4A7C15ull + seed;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        x[e] = (T)((double)(z >> 11) * 0x1p-53 * 8.0 - 4.0);
+    }
+}
+
+}  // namespace
+
+template <typename T>
+int tune_fit_variant(int64_t d, int64_t k_in, cudaStream_t s, int *variant) {
+    *variant = 0;
+    if (const char *e = std::getenv("KMC_TUNE"))
+        if (e[0] == '0') return KMC_OK;
+    if (d < 1 || k_in < 1) return KMC_OK;
+    int64_t k = 1;
+    while (k < k_in) k <<= 1;
+    const char *tag = sizeof(T) == 4 ? "fit-f32" : "fit-f64";
+    if (tune_lookup(d, k, tag, variant)) return KMC_OK;
+    const int n_var = sizeof(T) == 4 ? 3 : 2;
+    const int64_t n = 65536;
+    Scratch mem;
+    const size_t oX = 0, oC = oX + align256(sizeof(T) * n * d), oh = oC + align256(sizeof(T) * d * k);
+    const size_t ow = oh + align256(sizeof(T) * k), ol = ow + align256(sizeof(T) * n);
+    const size_t os = ol + align256(sizeof(int32_t) * n);
+    KMC_TRY(mem.alloc(os + align256(sizeof(double) * (d * k + k)), s));
+    char *b = mem.as<char>();
+    T *X = reinterpret_cast<T *>(b + oX), *C = reinterpret_cast<T *>(b + oC);
+    T *hn = reinterpret_cast<T *>(b + oh), *w = reinterpret_cast<T *>(b + ow);
+    int32_t *lab = reinterpret_cast<int32_t *>(b + ol);
+    double *sums = reinterpret_cast<double *>(b + os);
+    tune_fill_kernel<T><<<1024, 256, 0, s>>>(X, n * d, 11);
+    tune_fill_kernel<T><<<64, 256, 0, s>>>(C, d * k, 12);
+    KMC_TRY(check_launch("tune_fill"));
+    KMC_TRY(launch_fill<T>(w, T(1), n, s));
+    KMC_TRY(launch_half_norm<T>(C, hn, d, k, s));
+    cudaEvent_t e0, e1;
+    KMC_CUDA_TRY(cudaEventCreate(&e0));
+    KMC_CUDA_TRY(cudaEventCreate(&e1));
+    float best_ms = 0.f;
+    int best = 0, rc = KMC_OK;
+    for (int v = 0; v < n_var && rc == KMC_OK; ++v) {
+        float tot = 0.f;
+        for (int rep = 0; rep < 4 && rc == KMC_OK; ++rep) {
+            rc = launch_fill<double>(sums, 0.0, d * k + k, s);
+            if (rc == KMC_OK) rc = cudaEventRecord(e0, s) == cudaSuccess ? KMC_OK : KMC_ERR_CUDA;
+            if (rc == KMC_OK)
+                rc = launch_fused_step<T, int32_t, double>(X, w, C, hn, lab, sums, sums + d * k,
+                                                           n, d, k, 1, s, nullptr, v);
+            if (rc == KMC_OK) rc = cudaEventRecord(e1, s) == cudaSuccess ? KMC_OK : KMC_ERR_CUDA;
+            if (rc == KMC_OK) rc = cudaEventSynchronize(e1) == cudaSuccess ? KMC_OK : KMC_ERR_CUDA;
+            float ms = 0.f;
+            if (rc == KMC_OK)
+                rc = cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess ? KMC_OK : KMC_ERR_CUDA;
+            if (rep > 0) tot += ms;  // the first run warms up
+        }
+        if (v == 0 || tot < best_ms) {
+            best_ms = tot;
+            best = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != KMC_OK) {
+        set_error("tile autotuner: a timing launch failed");
+        return rc;
+    }
+    tune_record(d, k, tag, best);
+    *variant = best;
+    return KMC_OK;
+}
+
+template int tune_fit_variant<float>(int64_t, int64_t, cudaStream_t, int *);
+template int tune_fit_variant<double>(int64_t, int64_t, cudaStream_t, int *);
+
 #define KMC_INST_LLOYD(T, I)                                                                 \
     template int launch_assignment<T, I>(const T *, const T *, const T *, I *, int64_t,      \
-                                         int64_t, int64_t, cudaStream_t, const LoopState *); \
+                                         int64_t, int64_t, cudaStream_t, const LoopState *,  \
+                                         int);                                               \
     template int launch_fused_step<T, I, T>(const T *, const T *, const T *, const T *, I *,   \
                                             T *, T *, int64_t, int64_t, int64_t, int64_t,     \
-                                            cudaStream_t, const LoopState *);                 \
+                                            cudaStream_t, const LoopState *, int);            \
 
 
 template int launch_fused_step<float, int32_t, double>(const float *, const float *,
                                                        const float *, const float *, int32_t *,
                                                        double *, double *, int64_t, int64_t,
                                                        int64_t, int64_t, cudaStream_t,
-                                                       const LoopState *);
+                                                       const LoopState *, int);
 template int launch_fused_step<float, int64_t, double>(const float *, const float *,
                                                        const float *, const float *, int64_t *,
                                                        double *, double *, int64_t, int64_t,
                                                        int64_t, int64_t, cudaStream_t,
-                                                       const LoopState *);
+                                                       const LoopState *, int);
 KMC_INST_LLOYD(float, int32_t)
 KMC_INST_LLOYD(float, int64_t)
 KMC_INST_LLOYD(double, int32_t)

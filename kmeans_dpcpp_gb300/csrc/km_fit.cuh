@@ -72,6 +72,12 @@ struct FitBase {
         (void)stall;
         return KMC_OK;
     }
+    // Centroid-tile variant of the plain form's kernels (the autotuner's
+    // choice unless set here); the mixed forms ignore it.
+    virtual int set_tile_variant(int v) {
+        (void)v;
+        return KMC_OK;
+    }
     // Samples re-evaluated in exact arithmetic (mixed form): last pass and total.
     virtual int counters(int64_t *last, int64_t *total, int *device_error) {
         if (last) *last = 0;
@@ -96,7 +102,14 @@ struct PlainFit : FitBase {
     void *thr_scratch = nullptr, *sel_scratch = nullptr;
     int64_t issued = 0;
     int host_done = 0;
+    int tile_variant = 0;  // autotuned centroid-tile width of the plain kernels
     Scratch xt;  // feature-major copy of a row-major X (forms that need one)
+
+    int set_tile_variant(int v) override {
+        KMC_CHECK_ARG(v >= 0 && v <= 2, "tile variant must be 0, 1 or 2");
+        tile_variant = v;
+        return KMC_OK;
+    }
 
     int init(const FitParams<T, I> &p);
     int enqueue_iteration() override;

@@ -122,15 +122,29 @@ template <typename T>
 int launch_fill(T *p, T v, int64_t count, cudaStream_t s, const LoopState *guard = nullptr);
 
 // ---- kernels_lloyd.cu : SIMT tiled distance kernels (exact FP32/FP64) ----
+// variant: centroid-tile width of the autotuner (0: 16 x the default micro-
+// tile width, 1: half of it, 2: 32 columns); every variant computes each
+// (sample, centroid) score with the same arithmetic, so labels do not depend
+// on it.  Variants 1 and 2 of the fused step exist for float64 accumulators.
 template <typename T, typename I>
 int launch_assignment(const T *X, const T *C, const T *hn, I *labels, int64_t n, int64_t d,
-                      int64_t k, cudaStream_t s, const LoopState *guard = nullptr);
+                      int64_t k, cudaStream_t s, const LoopState *guard = nullptr,
+                      int variant = 0);
 // A: accumulator type of the private copies (dataT for the public API,
 // double inside the driver so sums are rounded to dataT once).
 template <typename T, typename I, typename A>
 int launch_fused_step(const T *X, const T *w, const T *C, const T *hn, I *labels, A *sums_cp,
                       A *sizes_cp, int64_t n, int64_t d, int64_t k, int64_t P, cudaStream_t s,
-                      const LoopState *guard = nullptr);
+                      const LoopState *guard = nullptr, int variant = 0);
+// Autotuner of the single-fit tile: times the fused step of each variant on a
+// synthetic 65,536-sample instance of (d, power-of-two bucket of k) once and
+// caches the fastest (in memory and in the tile cache file).  KMC_TUNE=0 in
+// the environment turns it off (variant 0).
+template <typename T>
+int tune_fit_variant(int64_t d, int64_t k, cudaStream_t s, int *variant);
+// The autotuner cache (batch_kernels.cu): choice for (d, k bucket, tag).
+bool tune_lookup(int64_t d, int64_t k, const char *tag, int *variant);
+void tune_record(int64_t d, int64_t k, const char *tag, int variant);
 template <typename T>
 int launch_distances(const T *X, const T *C, T *out, int64_t n, int64_t d, int64_t k,
                      cudaStream_t s);
