@@ -67,6 +67,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstring>
 
 #include "km_fit.cuh"
 #include "km_mixed.cuh"
@@ -96,7 +97,9 @@ struct MixedConsts {
     float sigma;
     unsigned int xmax_bits;  // max |x| (fp32 bits)
     int overflow;            // an operand left the 16-bit range this pass
-    int pad;
+    unsigned int wmax_bits;  // max |w| (fp32 bits; fixed-point sums only)
+    int fx_shift;            // w x and w are summed as the integers w x 2^fx_shift, w 2^fx_shift
+    int fx_ok;               // the fixed-point sums may be used (finite bounds)
 };
 
 struct MixedArgs {
@@ -137,10 +140,23 @@ struct MixedArgs {
     int64_t k_img, col0;
     int multi;
     float *pmax;
+    // > 0: the sums of own_k clusters are accumulated per CTA in shared memory
+    // (fixed point), own_f features per update thread
+    // as integers (fixed point), flushed once (d <= 32, one pass)
+    int64_t own_k;
+    int own_f;
+    const int *xq;  // [n][d4 + 4] packed fixed-point terms (w x, then w, 0, 0, 0)
 };
 
+// Fixed-point sums: each of the 64 update threads adds own_f consecutive
+// columns of its rows, w columns / own_f threads per row, so the rows are
+// split into (and the sums kept in) this many groups.
+__host__ __device__ constexpr int fx_copies(int64_t w, int own_f) {
+    return (int)(kUpdThreads / (w / own_f));
+}
+
 struct SmemLayout {
-    size_t c, hnb, aon, x, xch, lab, bar, p1, total;
+    size_t c, hnb, aon, x, xch, lab, bar, p1, osum, ostage, ocode, ow, total;
 };
 
 // Sub-chunk maxima stay in registers up to two chunks; beyond that they go
@@ -155,8 +171,13 @@ __host__ __device__ constexpr bool p1_in_smem(int64_t nch) { return nch >= 3; }
 // xch:  per-row maxima of the two column halves (two tiles in flight)
 // lab:  labels / recheck slots handed to the update warps (two tiles)
 // p1:   sub-chunk maxima, [sub-chunk][256 epilogue threads] (3+ chunks)
+// osum: the CTA's fixed-point cluster sums and sizes, R copies of
+//       [own_k + 1][d4 + 4] (int64), R = fx_copies(d4 + 4, own_f); ostage /
+//       ocode: a tile's packed rows and labels handed between the two update
+//       warps (fixed-point sums only)
 __host__ __device__ inline SmemLayout smem_layout(int nkb, int64_t k_pad, int64_t d4,
-                                                  int stages) {
+                                                  int stages, int64_t own_k = 0,
+                                                  int own_f = 1) {
     SmemLayout L;
     size_t off = 0;
     L.c = off;
@@ -179,6 +200,20 @@ __host__ __device__ inline SmemLayout smem_layout(int nkb, int64_t k_pad, int64_
     off = (off + 15) & ~size_t(15);
     L.p1 = off;
     if (p1_in_smem(k_pad / kChunkN)) off += sizeof(float) * 32 * kEpiWarps * (size_t)(k_pad / 64);
+    off = (off + 15) & ~size_t(15);
+    L.osum = off;
+    L.ostage = L.ocode = L.ow = off;
+    if (own_k > 0) {
+        // R copies of [own_k + 1][d4 + 4] (the last cluster row takes rows
+        // without a certified label)
+        off += sizeof(long long) * (size_t)fx_copies(d4 + 4, own_f) * (size_t)(own_k + 1) *
+               (size_t)(d4 + 4);
+        L.ostage = off;
+        off += sizeof(int) * kTileM * (size_t)(d4 + 4);
+        L.ocode = off;
+        off += sizeof(int) * kTileM;
+        L.ow = off;
+    }
     L.total = off + 1024;  // slack for aligning the dynamic shared memory base
     return L;
 }
@@ -272,6 +307,241 @@ __device__ __forceinline__ bool pair_any(bool v, int q) {
     return r != 0;
 }
 
+// Barrier of the two update warps (named barrier 12, 64 threads); upd_any
+// also returns the OR of v over them.
+__device__ __forceinline__ void upd_sync() {
+    asm volatile("bar.sync 12, 64;" ::: "memory");
+}
+__device__ __forceinline__ bool upd_any(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "barrier.red.or.pred q, 12, 64, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v)
+        : "memory");
+    return r != 0;
+}
+
+// 2^e as a float (e in [-126, 127]).
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
+
+// Packed fixed-point term of a float v = +-m 2^(E - 150) (E its exponent
+// field, m its 24-bit mantissa) at scale 2^s, emin = 150 - s: when
+// 0 <= E - emin <= 30, v 2^s = +-m 2^(E - emin) is an integer, stored as
+// (+-m) << 6 | (E - emin) << 1; zero is 0; every other v (below the scale's
+// resolution, denormal, infinite, NaN; the field 255 lies more than 30 above
+// any emin <= 224) is the flag 1, which adds nothing.
+__host__ __device__ inline int pack_fixed(float v, int emin) {
+    uint32_t b;
+    memcpy(&b, &v, 4);
+    if ((b & 0x7fffffffu) == 0u) return 0;
+    const uint32_t sh = (uint32_t)((int)((b >> 23) & 0xffu) - emin);
+    if (sh > 30u) return 1;
+    const int m = (int)((b & 0x7fffffu) | 0x800000u);
+    const int ms = (b >> 31) ? -m : m;
+    return (int)(((uint32_t)ms << 6) | (sh << 1));
+}
+
+// sum += the integer a packed term stands for (one 32 x 32 -> 64-bit
+// multiply-add).
+__device__ __forceinline__ void add_packed(unsigned long long &sum, int p) {
+    const int ms = p >> 6;
+    const int pw = 1 << ((p >> 1) & 31);
+    asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(sum) : "r"(ms), "r"(pw));
+}
+
+// own_f consecutive 64-bit sums at a shared-window address (16-byte aligned
+// for own_f >= 2).
+template <int F>
+__device__ __forceinline__ void lds_sums(uint32_t addr, unsigned long long (&q)[F]) {
+    if constexpr (F == 1) {
+        q[0] = lds_b64(addr);
+    } else {
+#pragma unroll
+        for (int j = 0; j < F; j += 2)
+            asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(q[j]), "=l"(q[j + 1]) : "r"(addr + 8u * j));
+    }
+}
+template <int F>
+__device__ __forceinline__ void sts_sums(uint32_t addr, const unsigned long long (&q)[F]) {
+    if constexpr (F == 1) {
+        sts_b64(addr, q[0]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < F; j += 2)
+            asm volatile("st.shared.v2.u64 [%0], {%1, %2};" ::"r"(addr + 8u * j), "l"(q[j]), "l"(q[j + 1]));
+    }
+}
+
+// Second pass over a tile's terms that the fixed-point sums cannot hold
+// (flag 1: below the scale's resolution, or NaN): their exact float values
+// straight into the float64 sums.  Kept out of line so that no float64
+// instruction enters the first pass.  Columns c0 .. c0 + nc - 1 of rows
+// grp, grp + R, ... of the tile whose first sample is i0.
+__device__ __noinline__ void rare_terms(const MixedArgs &a, double *acc64, int64_t ks, int64_t i0,
+                                        const int *code, const int *stage, int grp, int R, int c0,
+                                        int nc) {
+    const int64_t d4 = a.d4, ds = d4 + 4;
+    for (int r = grp; r < kTileM; r += R) {
+        const int c = code[r];
+        if (c < 0 || c >= a.k) continue;
+        for (int j = c0; j < c0 + nc; ++j) {
+            if (stage[r * ds + j] != 1) continue;
+            const float w = a.w[i0 + r];
+            if (j < d4) {
+                const float v = __fmul_rn(a.xrow[(i0 + r) * d4 + j], w);
+                if (v != 0.f) atomicAdd(acc64 + (int64_t)c * d4 + j, (double)v);
+            } else if (j == d4) {
+                atomicAdd(acc64 + ks * d4 + c, (double)w);
+            }
+        }
+    }
+}
+
+// The update role of the tensor-core kernel with fixed-point sums (d <= 32,
+// one column pass): the CTA adds the features and weights of its certified
+// rows into integer sums in shared memory and reduces them into its global
+// float64 copy once at the end.  Every term w x (and w) is prepared once per
+// fit as the packed integer w x 2^fx_shift (the shift keeps every CTA's sums
+// below 2^61), so a term costs one multiply-add on the integer pipe per
+// iteration.  No float64 instruction runs per tile: on this part even a
+// predicated-off float64 conversion costs the issue slots of a whole row.
+// Terms below the scale's resolution, and NaNs, are rare: a tile that has
+// some adds them to the float64 copy in a second pass.
+//
+// Rows are d4 + 4 packed columns (w x_0 .. w x_{d4-1}, w, 0, 0, 0).  Thread
+// u adds columns j0 .. j0 + F - 1, j0 = F (u mod T), T = (d4 + 4) / F, of
+// rows r = g (mod R), g = u / T, R = fx_copies(d4 + 4, F), into its group's
+// copy [g][cluster][column]; rows without a certified label go to the spare
+// cluster row own_k.  The two update warps copy each tile's packed rows and
+// labels into shared memory (named barrier 12) and load the next tile's rows
+// while they add this one's.
+template <int F>
+__device__ __forceinline__ void fixed_sums_role(const MixedArgs &a, const MixedConsts &cst,
+                                                uint8_t *smem, const SmemLayout &L, int *lab_s,
+                                                uint64_t *ufull, uint64_t *uempty, volatile int *err,
+                                                long long lim, double *acc64, int64_t ks) {
+    const int u = threadIdx.x - 32 * (2 + kEpiWarps);
+    const int64_t n = a.n, k = a.k, d4 = a.d4, ok = a.own_k;
+    const int ds = (int)d4 + 4, dq = ds / 4;  // packed columns, uint4 per row
+    const int64_t ntiles = ceil_div<int64_t>(n, kTileM);
+    const int T = ds / F, R = fx_copies(ds, F);
+    const int grp = u / T, j0 = F * (u - grp * T);
+    long long *osum = reinterpret_cast<long long *>(smem + L.osum);
+    int *ostage = reinterpret_cast<int *>(smem + L.ostage);
+    int *ocode = reinterpret_cast<int *>(smem + L.ocode);
+    const uint32_t mine = smem_u32(osum + (int64_t)grp * (ok + 1) * ds + j0);
+    const uint32_t cstride = 8u * (uint32_t)ds;
+
+    for (int64_t e = u; e < (int64_t)R * (ok + 1) * ds; e += kUpdThreads) osum[e] = 0;
+    // rows u and u + 64 of a tile, loaded one tile ahead
+    uint4 ra[9], rb[9];
+    auto load_rows = [&](int64_t tile) {
+        const int64_t i0 = tile * kTileM + u, i1 = i0 + 64;
+        const uint4 *pa = reinterpret_cast<const uint4 *>(a.xq + i0 * ds);
+        const uint4 *pb = reinterpret_cast<const uint4 *>(a.xq + i1 * ds);
+#pragma unroll
+        for (int g = 0; g < 9; ++g) {
+            const bool in = g < dq && tile < ntiles;
+            ra[g] = (in && i0 < n) ? __ldg(pa + g) : make_uint4(0u, 0u, 0u, 0u);
+            rb[g] = (in && i1 < n) ? __ldg(pb + g) : make_uint4(0u, 0u, 0u, 0u);
+        }
+    };
+    load_rows(blockIdx.x);
+    int tl = 0;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tl) {
+        const int tb = tl & 1;
+        const bool got = mbar_wait(&ufull[tb], ((uint32_t)tl >> 1) & 1u, err, lim);
+        int c0 = -1, c1 = -1;
+        if (got) {
+            c0 = lab_s[tb * kTileM + u];
+            c1 = lab_s[tb * kTileM + u + 64];
+            mbar_arrive(&uempty[tb]);
+        }
+        // both warps stop together (this barrier also orders the previous
+        // tile's reads of the stage before the writes below)
+        if (upd_any(!got)) break;
+        uint4 *sa = reinterpret_cast<uint4 *>(ostage + u * ds);
+        uint4 *sb = reinterpret_cast<uint4 *>(ostage + (u + 64) * ds);
+#pragma unroll
+        for (int g = 0; g < 9; ++g)
+            if (g < dq) {
+                sa[g] = ra[g];
+                sb[g] = rb[g];
+            }
+        // labels of rows the kernel did not certify (and padding) go to the
+        // spare cluster row
+        ocode[u] = (c0 >= 0 && c0 < k) ? c0 : (int)ok;
+        ocode[u + 64] = (c1 >= 0 && c1 < k) ? c1 : (int)ok;
+        upd_sync();
+        load_rows(tile + gridDim.x);
+        if (grp < R) {
+            int flags = 0;
+            for (int r = grp; r < kTileM; r += R) {
+                const int c = ocode[r];
+                const int *t = ostage + r * ds + j0;
+                int v[F];
+                if constexpr (F == 4) {
+                    const int4 q = *reinterpret_cast<const int4 *>(t);
+                    v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+                } else if constexpr (F == 2) {
+                    const int2 q = *reinterpret_cast<const int2 *>(t);
+                    v[0] = q.x, v[1] = q.y;
+                } else {
+                    v[0] = t[0];
+                }
+                const uint32_t addr = mine + (uint32_t)c * cstride;
+                unsigned long long sum[F];
+                lds_sums<F>(addr, sum);
+                int rf = 0;
+#pragma unroll
+                for (int j = 0; j < F; ++j) {
+                    add_packed(sum[j], v[j]);
+                    rf |= v[j];
+                }
+                sts_sums<F>(addr, sum);
+                // flagged terms of the spare row never count
+                flags |= c != (int)ok ? rf : 0;
+            }
+            if (flags & 1)
+                rare_terms(a, acc64, ks, tile * kTileM, ocode, ostage, grp, R, j0, F);
+        }
+    }
+    upd_sync();
+    // this CTA's sums (its R copies added exactly) into its global float64
+    // copy (copies may be shared by several CTAs: reductions)
+    const double sc = 1.0 / (double)pow2f(cst.fx_shift);  // a power of two
+    for (int64_t e = u; e < ok * (d4 + 1); e += kUpdThreads) {
+        const int64_t c = e < ok * d4 ? e / d4 : e - ok * d4;
+        const int64_t j = e < ok * d4 ? e - c * d4 : d4;
+        long long q = 0;
+        for (int g = 0; g < R; ++g) q += osum[((int64_t)g * (ok + 1) + c) * ds + j];
+        if (q != 0) atomicAdd(e < ok * d4 ? acc64 + e : acc64 + ks * d4 + c, __ll2double_rn(q) * sc);
+    }
+}
+
+// Packed fixed-point terms of every sample: w x_j for j < d4 (rounded
+// products, as the reference forms them), then w, 0, 0, 0.
+__global__ void fx_pack_kernel(const float *xrow, const float *w, int64_t n, int64_t d4,
+                               const MixedConsts *c, int *xq) {
+    const int64_t ds = d4 + 4;
+    const int emin = 150 - c->fx_shift;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n * ds;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e / ds, j = e - i * ds;
+        const float wi = w[i];
+        float v = 0.f;
+        if (j < d4)
+            v = __fmul_rn(xrow[i * d4 + j], wi);
+        else if (j == d4)
+            v = wi;
+        xq[e] = pack_fixed(v, emin);
+    }
+}
+
 template <int BF16>
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
     if (BF16) {
@@ -298,7 +568,7 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
     uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     constexpr int64_t k_pad = (int64_t)NCH * kChunkN;
     const int stages = a.stages;
-    const SmemLayout L = smem_layout(NKB, k_pad, a.d4, stages);
+    const SmemLayout L = smem_layout(NKB, k_pad, a.d4, stages, a.own_k, a.own_f);
     uint8_t *cimg_s = smem + L.c;
     uint8_t *aon_s = smem + L.aon;
     uint8_t *xring = smem + L.x;
@@ -690,8 +960,18 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
                 if (pass == 0) atomicAdd(sums32 + ks * d4 + code, wv);
             }
         };
+        bool owned_done = false;
+        if constexpr (NKB == 1 && !MULTI) {
+            if (a.update && a.own_k > 0 && cst.fx_ok) {
+                if (a.own_f == 4)
+                    fixed_sums_role<4>(a, cst, smem, L, lab_s, ufull, uempty, err, lim, acc64, ks);
+                else
+                    fixed_sums_role<2>(a, cst, smem, L, lab_s, ufull, uempty, err, lim, acc64, ks);
+                owned_done = true;
+            }
+        }
         int tl = 0;
-        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tl) {
+        for (int64_t tile = blockIdx.x; !owned_done && tile < ntiles; tile += gridDim.x, ++tl) {
             const int tb = tl & 1;
             const int64_t i0 = tile * kTileM + u, i1 = i0 + 64;
             const float w0 = (a.update && i0 < n) ? __ldg(a.w + i0) : 0.f;
@@ -769,6 +1049,30 @@ __global__ void sigma_kernel(MixedConsts *c, int bf16, int64_t d) {
     c->sigma = (float)sigma;
     c->s2 = (float)(sigma * sigma);
     c->overflow = 0;
+}
+
+// Shift of the fixed-point cluster sums: a CTA adds at most `rows` (>= 128)
+// values w x per feature (|w x| <= max|x| max|w|) and `rows` weights, so with
+// bound = rows max(max|x| max|w|, max|w|) < 2^e the shift 61 - e keeps every
+// sum below 2^61 and every term below 2^54 (all-zero data gives 0).
+__global__ void fixed_scale_kernel(MixedConsts *c, double rows) {
+    const double xm = (double)__uint_as_float(c->xmax_bits);
+    const double wm = (double)__uint_as_float(c->wmax_bits);
+    auto shift_for = [](double bound) {
+        int sh = 0;
+        if (bound > 0.0 && bound < 1e300) {
+            int e = 0;
+            frexp(bound, &e);
+            sh = min(100, 61 - e);
+        }
+        return sh;
+    };
+    const int sx = shift_for(rows * fmax(xm * wm, wm));
+    // products w x that may overflow fp32, and scales whose resolution field
+    // 150 - shift would come within 30 of the infinity / NaN field, keep the
+    // float64 reductions
+    c->fx_ok = (xm * wm < 1e37 && sx >= -70) ? 1 : 0;
+    c->fx_shift = sx;
 }
 
 // Round to the 16-bit operand type and back (exact in fp32).
@@ -1430,6 +1734,9 @@ struct MixedFit : PlainFit<float, I> {
     int nch = 1;     // 256-column chunks per pass
     int passes = 1;  // column passes per assignment (n_clusters beyond one pass)
     float *pmax = nullptr;
+    int64_t own_k = 0;  // > 0: fixed-point sums accumulated per CTA in shared memory
+    int own_f = 1;      // packed columns per update thread in those sums
+    int *xq = nullptr;  // [n][d4 + 4] packed fixed-point terms
 
     static bool supported(int64_t d, int64_t k) {
         const int nk = (int)ceil_div<int64_t>(std::max<int64_t>(d, 1), 64);
@@ -1458,6 +1765,23 @@ struct MixedFit : PlainFit<float, I> {
         // (a few per sample; they keep the trajectory on the float64
         // reference's), beyond that float32 four-wide reductions.
         acc_f64 = d4 <= 32 ? 1 : 0;
+        // float64 sums that fit shared memory next to the operands (keeping a
+        // ring of at least two stages) are formed per CTA in fixed point: the
+        // deepest ring that fits, then as many columns per update thread as
+        // fit beside it.  One column per thread leaves a single copy, whose
+        // read-modify-write chain (one row after another) is slower than the
+        // float64 reductions.  Fits only: a prediction has no weights and no
+        // sums.
+        if (acc_f64 && passes == 1 && p.w != nullptr) {
+            for (int st = stages; st >= 2 && own_k == 0; --st)
+                for (int f : {4, 2})
+                    if (smem_layout(nkb, k_pad, d4, st, p.k, f).total <= kSmemLimit) {
+                        own_k = p.k;
+                        own_f = f;
+                        stages = st;
+                        break;
+                    }
+        }
         size_t off = 0;
         auto take = [&](size_t bytes) {
             size_t o = off;
@@ -1483,6 +1807,7 @@ struct MixedFit : PlainFit<float, I> {
         const size_t o_s32 = take(acc_f64 ? 16 : sizeof(float) * csz);
         const size_t o_a64 = take(acc_f64 ? sizeof(double) * csz : 16);
         const size_t o_xf = take(sizeof(float) * std::max<int64_t>(p.n, 1) * d4);
+        const size_t o_xq = take(own_k > 0 ? sizeof(int) * std::max<int64_t>(p.n, 1) * (d4 + 4) : 16);
         const size_t o_cn2 = take(sizeof(float) * p.k);
         const size_t o_dcn = take(sizeof(float) * p.k);
         const size_t o_cst = take(sizeof(MixedConsts));
@@ -1502,6 +1827,7 @@ struct MixedFit : PlainFit<float, I> {
         sums32 = reinterpret_cast<float *>(b + o_s32);
         acc64 = reinterpret_cast<double *>(b + o_a64);
         xrow = reinterpret_cast<float *>(b + o_xf);
+        xq = reinterpret_cast<int *>(b + o_xq);
         cn2 = reinterpret_cast<float *>(b + o_cn2);
         dcn = reinterpret_cast<float *>(b + o_dcn);
         consts = reinterpret_cast<MixedConsts *>(b + o_cst);
@@ -1520,6 +1846,16 @@ struct MixedFit : PlainFit<float, I> {
         KMC_TRY(check_launch("absmax"));
         sigma_kernel<<<1, 1, 0, s>>>(consts, bf16, p.d);
         KMC_TRY(check_launch("sigma"));
+        if (own_k > 0) {
+            absmax_kernel<<<grid1d(p.n, 256, 4096), 256, 0, s>>>(p.w, p.n, &consts->wmax_bits);
+            KMC_TRY(check_launch("absmax_w"));
+            // rows one CTA of the assignment handles at most
+            const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(ntiles, num_sms()));
+            const double rows = (double)ceil_div<int64_t>(std::max<int64_t>(ntiles, 1), grid) * kTileM;
+            fixed_scale_kernel<<<1, 1, 0, s>>>(consts, rows);
+            KMC_TRY(check_launch("fixed_scale"));
+            this->launches += 2;
+        }
         {
             auto xk = bf16 ? x_image_kernel<1> : x_image_kernel<0>;
             const size_t xsm = x_image_smem(nkb);
@@ -1532,6 +1868,12 @@ struct MixedFit : PlainFit<float, I> {
         }
         KMC_TRY(check_launch("x_image"));
         this->launches += 3;
+        if (own_k > 0) {
+            fx_pack_kernel<<<grid1d(p.n * (d4 + 4), 256, 8192), 256, 0, s>>>(xrow, p.w, p.n, d4,
+                                                                           consts, xq);
+            KMC_TRY(check_launch("fx_pack"));
+            this->launches += 1;
+        }
         return KMC_OK;
     }
 
@@ -1594,7 +1936,14 @@ struct MixedFit : PlainFit<float, I> {
         a.k_img = k_pad;
         a.multi = passes > 1 ? 1 : 0;
         if (a.multi) a.update = 0;  // the combine accumulates the certified samples
-        const SmemLayout L = smem_layout(nkb, pass_cols, d4, stages);
+        a.own_k = a.multi ? 0 : own_k;
+        a.own_f = own_f;
+        a.xq = xq;
+        const SmemLayout L = smem_layout(nkb, pass_cols, d4, stages, a.own_k, a.own_f);
+        if ((L.ostage & 15) != 0 || (L.osum & 15) != 0) {
+            set_error("mixed form: misaligned shared-memory sums layout");
+            return KMC_ERR_CUDA;
+        }
         auto kern = pick_kernel(bf16, nkb, nch, a.multi != 0);
         if (kern == nullptr) {
             set_error("mixed form: no kernel for %d feature blocks and %d chunks", nkb, nch);

@@ -186,6 +186,54 @@ def test_mixed_iterations_match_oracle_step_by_step(oracle, case, form):
     assert inertia.value == pytest.approx(inr_o, rel=1e-6)
 
 
+# Up to 32 features the tensor-core kernel adds the cluster sums as integers
+# (fixed point, scaled by the data's bounds); values below that scale's
+# resolution (a feature a trillion times smaller than the rest, weights of
+# 1e-30) take a float64 side path.  Every centroid coordinate must still follow
+# the oracle on its own scale.
+@pytest.mark.parametrize("d,k", [(8, 8), (20, 40), (32, 64)])
+@pytest.mark.parametrize("form", sorted(FORMS))
+def test_mixed_fixed_point_sums_with_tiny_values_and_weights(oracle, d, k, form):
+    import torch
+
+    from kmeans_dpcpp_gb300 import capi
+
+    n, iters = 30_000, 3
+    X, _, _ = bench.make_blobs(n, d, k, (-5, 5), 1.0, 11)
+    X = np.ascontiguousarray(X)
+    X[0] *= np.float32(1e-12)
+    rng = np.random.default_rng(11)
+    w = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    w[rng.choice(n, 300, replace=False)] = np.float32(1e-30)
+    w[rng.choice(n, 300, replace=False)] = 0.0
+    C0 = np.ascontiguousarray(bench.random_row_init(X, k, 11))
+    L = capi.lib()
+    Xg = torch.from_numpy(X).cuda()
+    wg = torch.from_numpy(w).cuda()
+    cur = torch.from_numpy(C0.copy()).cuda()
+    res = torch.empty_like(cur)
+    lab = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    fit = ctypes.c_void_p()
+    capi.check(L.kmc_fit_create_f32_i32(Xg.data_ptr(), wg.data_ptr(), cur.data_ptr(), lab.data_ptr(),
+                                        res.data_ptr(), n, d, k, 0.0, iters, FORMS[form],
+                                        stream.cuda_stream, ctypes.byref(fit)))
+    try:
+        for _ in range(iters):
+            C_before = cur.cpu().numpy().copy()
+            capi.check(L.kmc_fit_step(fit, 1))
+            stream.synchronize()
+            np.testing.assert_array_equal(lab.cpu().numpy(), oracle.assignment(X, C_before))
+            _, _, C_o, _, _ = oracle.kmeans_lloyd_driver(X, w, C_before, 0.0, 1)
+            C_after = cur.cpu().numpy()
+            for f in range(d):
+                scale = float(np.abs(C_o[f]).max())
+                np.testing.assert_allclose(C_after[f], C_o[f], rtol=1e-6, atol=1e-6 * scale,
+                                           err_msg=f"feature {f}")
+    finally:
+        capi.check(L.kmc_fit_destroy(fit))
+
+
 def test_fit_after_trimming_the_memory_pool_gives_the_same_labels(oracle):
     """Scratch comes from a pool that keeps freed memory mapped; trimming it
     between fits hands the memory back and the next fit allocates afresh."""
