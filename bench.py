@@ -619,9 +619,64 @@ def run_c4(args, world, rank, local):
             t += time.perf_counter() - t0
         return t
 
+    def served_mixed():
+        # the mixed form's batched path: the request server runs the fits as
+        # concurrent graph-replayed tensor-core sessions
+        srv = ctypes.c_void_p()
+        capi.check(L.kmc_server_open(FORMS["mixed-fp16"], 150 * 10 ** 9, len(inst), s, ctypes.byref(srv)))
+        keep, tickets = [], []
+        try:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for (n, d, k, _), (X, C0) in zip(inst, data):
+                lab = torch.empty(n, dtype=torch.int32, device="cuda")
+                Cout = torch.empty_like(C0)
+                keep.append((lab, Cout))
+                q = ctypes.c_int64()
+                capi.check(L.kmc_server_submit_fit_f32(srv, X.data_ptr(), w_all[n].data_ptr(), C0.data_ptr(),
+                                                       lab.data_ptr(), Cout.data_ptr(), n, d, k, 0.0, iters,
+                                                       ctypes.byref(q)))
+                tickets.append(q.value)
+            done_iters = 0
+            for q in tickets:
+                st, it, inr = ctypes.c_int(), ctypes.c_int64(), ctypes.c_double()
+                capi.check(L.kmc_server_wait(srv, q, ctypes.byref(st), ctypes.byref(it), ctypes.byref(inr)))
+                capi.check(st.value)
+                done_iters += it.value
+            torch.cuda.synchronize()
+            return time.perf_counter() - t0, done_iters
+        finally:
+            capi.check(L.kmc_server_close(srv))
+
+    def single_mixed_loop():
+        t, done_iters = 0.0, 0
+        for (n, d, k, _), (X, C0) in zip(inst, data):
+            C = C0.clone()
+            res = torch.empty_like(C)
+            lab = torch.empty(n, dtype=torch.int32, device="cuda")
+            fit = ctypes.c_void_p()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            capi.check(L.kmc_fit_create_f32_i32(X.data_ptr(), w_all[n].data_ptr(), C.data_ptr(),
+                                                lab.data_ptr(), res.data_ptr(), n, d, k, 0.0, iters,
+                                                FORMS["mixed-fp16"], s, ctypes.byref(fit)))
+            try:
+                capi.check(L.kmc_fit_run(fit))
+                it, inr = ctypes.c_int64(), ctypes.c_double()
+                capi.check(L.kmc_fit_finalize(fit, ctypes.byref(it), ctypes.byref(inr)))
+                done_iters += it.value
+            finally:
+                capi.check(L.kmc_fit_destroy(fit))
+            torch.cuda.synchronize()
+            t += time.perf_counter() - t0
+        return t, done_iters
+
     batched()  # warm-up: allocator pools, graphs, kernel attributes
     t_batch = batched()
     t_single = single_loop()
+    served_mixed()  # warm-up
+    t_mixed, it_mixed = served_mixed()
+    t_mixed_single, it_mixed_single = single_mixed_loop()
     total = len(inst) * iters
     flops = sum(2.0 * n * k * d for (n, d, k, _) in inst) * iters
     line = {"metric": "batched fits: instance-iterations/s (c4)", "value": total / t_batch,
@@ -633,7 +688,13 @@ def run_c4(args, world, rank, local):
             "distance_tflops": flops / t_batch / 1e12,
             "single_fit_loop": {"value": total / t_single, "seconds": t_single},
             "speedup_vs_single_fit_loop": t_single / t_batch,
-            "batched_seconds": t_batch}
+            "batched_seconds": t_batch,
+            "mixed_fp16": {"value": it_mixed / t_mixed, "unit": "instance-iter/s", "seconds": t_mixed,
+                           "instance_iterations": it_mixed,
+                           "path": "request server: concurrent graph-replayed tensor-core sessions",
+                           "single_fit_loop": {"value": it_mixed_single / t_mixed_single,
+                                               "seconds": t_mixed_single},
+                           "speedup_vs_single_fit_loop": (it_mixed / t_mixed) / (it_mixed_single / t_mixed_single)}}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -141,8 +141,7 @@ struct MixedArgs {
     int multi;
     float *pmax;
     // > 0: the sums of own_k clusters are accumulated per CTA in shared memory
-    // (fixed point), own_f features per update thread
-    // as integers (fixed point), flushed once (d <= 32, one pass)
+    // (fixed point), own_f packed columns per update thread
     int64_t own_k;
     int own_f;
     const int *xq;  // [n][d4 + 4] packed fixed-point terms (w x, then w, 0, 0, 0)
@@ -832,7 +831,10 @@ __global__ void __launch_bounds__(kThreadsMixed, 1) mixed_assign_kernel(MixedArg
             // class of the winning half do (two distinct columns of one
             // sub-chunk lie in distinct classes).
             const float thr = fmaxf(Mh, Mo) - E2;
-            const bool win = (Mh > Mo) || (Mh == Mo && h == 0);
+            // exactly one of the pair wins, whatever the maxima (a NaN loses
+            // every comparison: the first half then wins); only the winner
+            // hands the row over, and ufull counts one arrival per row
+            const bool win = (Mh > Mo) || (h == 0 && !(Mo > Mh));
             uint32_t hot1 = 0u, hot2 = 0u;
             const HotTest ht = hot_test(thr);
             if (ht.ok) {

@@ -58,30 +58,35 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
                  : "memory");
 }
 
-// try_wait suspends the thread in hardware until the phase completes or the
-// suspend-time hint (ns) expires, so waiting warps do not spin on the issue
-// slots the working warps need.
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+// Non-blocking test of the phase with the given parity.  The waits below poll
+// it with a short sleep between polls.  The suspending form
+// (mbarrier.try_wait with a suspend-time hint) is not used: with tensor-core
+// kernels of several streams running at once, a thread suspended in it
+// sometimes stayed asleep for seconds after the phase had completed (fits of
+// the request server gave up their waits after the 2 s limit; with polling
+// none did).
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "mbarrier.test_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity), "r"(1000000u)
+        : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     return ok != 0;
 }
 
 // Waits for the phase with the given parity.  Returns false (and raises the
 // CTA error flag) after `limit` SM clocks, or as soon as another role has
-// raised the flag.
+// raised the flag.  After a few polls the waiter sleeps ~0.1 us between
+// polls, so waiting warps leave the issue slots to the working ones.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *err,
                                           long long limit = kWaitClocks) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_test(bar, parity)) return true;
     const long long t0 = clock64();
     while (true) {
-        if (mbar_try_wait(bar, parity)) return true;
+        if (mbar_test(bar, parity)) return true;
         if (*err) return false;
         if (clock64() - t0 > limit) {
             *err = 1;
@@ -96,10 +101,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
 // committed tensor-core operations -- which always completes, so a CTA never
 // frees TMEM or exits with such work still writing.
 __device__ __forceinline__ bool mbar_wait_drain(uint64_t *bar, uint32_t parity, volatile int *err) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_test(bar, parity)) return true;
     const long long t0 = clock64();
     while (true) {
-        if (mbar_try_wait(bar, parity)) return true;
+        if (mbar_test(bar, parity)) return true;
         if (clock64() - t0 > kWaitClocks) {
             *err = 1;
             return false;

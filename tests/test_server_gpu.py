@@ -247,3 +247,53 @@ def test_budget_and_invalid_calls():
         capi.check(L.kmc_server_close(srv))
     bad = ctypes.c_void_p()
     assert L.kmc_server_open(7, 1 << 30, 4, None, ctypes.byref(bad)) == ERR_INVALID
+
+
+def test_many_concurrent_mixed_sessions_all_finish_and_match_single_fits():
+    """Dozens of tensor-core sessions of small, uneven fits run at once (their
+    kernels on several streams).  Every fit must finish without a device-side
+    wait running out, and up to 32 features (exact sums) give the same labels
+    and centroids as the same fit run alone."""
+    import torch
+
+    from kmeans_dpcpp_gb300 import capi
+
+    L = capi.lib()
+    rng = np.random.default_rng(21)
+    reqs = []
+    for i in range(48):
+        n = int(np.exp(rng.uniform(np.log(2_000), np.log(200_000))))
+        d = int(rng.choice([8, 16, 32, 64]))
+        k = int(min(np.exp(rng.uniform(np.log(4), np.log(160))), n))
+        X, _, _ = bench.make_blobs(n, d, k, (-10, 10), 1.0, 100 + i)
+        C0 = np.ascontiguousarray(bench.random_row_init(X, k, 100 + i))
+        reqs.append(Req(0, np.ascontiguousarray(X), C0, tol=0.0, max_iter=15))
+    srv = _open(L, capi, "fp16", max_active=len(reqs))
+    try:
+        for r in reqs:
+            capi.check(r.submit(L, srv))
+        for r in reqs:
+            st, it, _ = _wait(L, capi, srv, r)
+            assert st == 0, (st, r.n, r.d, r.k, L.kmc_last_error().decode())
+    finally:
+        capi.check(L.kmc_server_close(srv))
+    stream = torch.cuda.current_stream()
+    for r in reqs:
+        if r.d > 32:
+            continue
+        C = torch.from_numpy(r.C0h.copy()).cuda()
+        res = torch.empty_like(C)
+        lab = torch.empty(r.n, dtype=torch.int32, device="cuda")
+        fit = ctypes.c_void_p()
+        capi.check(L.kmc_fit_create_f32_i32(r.X.data_ptr(), r.w.data_ptr(), C.data_ptr(), lab.data_ptr(),
+                                            res.data_ptr(), r.n, r.d, r.k, 0.0, 15, FORMS["fp16"],
+                                            stream.cuda_stream, ctypes.byref(fit)))
+        try:
+            capi.check(L.kmc_fit_run(fit))
+            it, inr = ctypes.c_int64(), ctypes.c_double()
+            capi.check(L.kmc_fit_finalize(fit, ctypes.byref(it), ctypes.byref(inr)))
+        finally:
+            capi.check(L.kmc_fit_destroy(fit))
+        out = r.result()
+        np.testing.assert_array_equal(out["labels"], lab.cpu().numpy())
+        np.testing.assert_allclose(out["C"], res.cpu().numpy(), rtol=1e-6, atol=1e-6)
