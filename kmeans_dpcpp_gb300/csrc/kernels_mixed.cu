@@ -102,6 +102,36 @@ struct MixedConsts {
     int fx_ok;               // the fixed-point sums may be used (finite bounds)
 };
 
+// Order-independent totals of the fixed-point sums (d <= 32): element e
+// (cluster-major [k][d4] sums, then the k sizes) of copy c is
+// hi[c stride + e] 2^32 + lo[c stride + e]; contributions q are added as
+// (q >> 32) into hi and (q mod 2^32) into lo with 64-bit integer atomics (the
+// copies, CTA b into copy b mod copies, spread the contention), and the copies
+// are added as integers, so every order gives the same bits.  xq: the packed
+// terms ([n][d4 + 4]); null when not in use.
+struct FxAcc {
+    const int *xq;
+    long long *hi;
+    unsigned long long *lo;
+    int64_t stride;  // elements per copy
+    int copies;
+    // the copy of block b
+    __device__ __forceinline__ FxAcc copy_of(unsigned b) const {
+        FxAcc r = *this;
+        if (hi != nullptr) {
+            const int64_t o = (int64_t)(b % (unsigned)copies) * stride;
+            r.hi += o;
+            r.lo += o;
+        }
+        return r;
+    }
+};
+
+__device__ __forceinline__ void fx_add(const FxAcc &fx, int64_t e, long long q) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(fx.hi + e), (unsigned long long)(q >> 32));
+    atomicAdd(fx.lo + e, (unsigned long long)(q & 0xffffffffll));
+}
+
 struct MixedArgs {
     const uint8_t *ximg;
     const uint8_t *cimg;
@@ -145,6 +175,7 @@ struct MixedArgs {
     int64_t own_k;
     int own_f;
     const int *xq;  // [n][d4 + 4] packed fixed-point terms (w x, then w, 0, 0, 0)
+    FxAcc fx;       // their order-independent totals
 };
 
 // Fixed-point sums: each of the 64 update threads adds own_f consecutive
@@ -402,8 +433,8 @@ __device__ __noinline__ void rare_terms(const MixedArgs &a, double *acc64, int64
 
 // The update role of the tensor-core kernel with fixed-point sums (d <= 32,
 // one column pass): the CTA adds the features and weights of its certified
-// rows into integer sums in shared memory and reduces them into its global
-// float64 copy once at the end.  Every term w x (and w) is prepared once per
+// rows into integer sums in shared memory and adds them to the fit's
+// order-independent integer totals (FxAcc) once at the end.  Every term w x (and w) is prepared once per
 // fit as the packed integer w x 2^fx_shift (the shift keeps every CTA's sums
 // below 2^61), so a term costs one multiply-add on the integer pipe per
 // iteration.  No float64 instruction runs per tile: on this part even a
@@ -510,15 +541,15 @@ __device__ __forceinline__ void fixed_sums_role(const MixedArgs &a, const MixedC
         }
     }
     upd_sync();
-    // this CTA's sums (its R copies added exactly) into its global float64
-    // copy (copies may be shared by several CTAs: reductions)
-    const double sc = 1.0 / (double)pow2f(cst.fx_shift);  // a power of two
+    // this CTA's sums (its R copies added exactly) into the order-independent
+    // integer totals
+    const FxAcc fxc = a.fx.copy_of(blockIdx.x);
     for (int64_t e = u; e < ok * (d4 + 1); e += kUpdThreads) {
         const int64_t c = e < ok * d4 ? e / d4 : e - ok * d4;
         const int64_t j = e < ok * d4 ? e - c * d4 : d4;
         long long q = 0;
         for (int g = 0; g < R; ++g) q += osum[((int64_t)g * (ok + 1) + c) * ds + j];
-        if (q != 0) atomicAdd(e < ok * d4 ? acc64 + e : acc64 + ks * d4 + c, __ll2double_rn(q) * sc);
+        if (q != 0) fx_add(fxc, e, q);
     }
 }
 
@@ -1352,9 +1383,12 @@ __global__ void __launch_bounds__(kRecheckThreads) recheck_kernel(
     const float *xrow, const float *ct, const float *hn, const float *w, const uint4 *cand,
     const int *flagged, const int *n_flagged, int64_t n, int64_t d, int64_t k, int64_t d4,
     void *labels, int label64, int update, int acc_f64, float *sums32, double *acc64,
-    int64_t k_pad, int n_copies, const LoopState *guard, int passes, int64_t pass_cols) {
+    int64_t k_pad, int n_copies, const LoopState *guard, int passes, int64_t pass_cols, FxAcc fx,
+    const MixedConsts *consts) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
     constexpr int kWarps = kRecheckThreads / 32;
+    const bool use_fx = fx.xq != nullptr && consts->fx_ok;
+    fx = fx.copy_of(blockIdx.x);
     __shared__ unsigned long long key_s[kWarps][32];
     __shared__ int incl_s[kWarps][32];
     __shared__ int row_s[kWarps][32];
@@ -1457,7 +1491,23 @@ __global__ void __launch_bounds__(kRecheckThreads) recheck_kernel(
                 reinterpret_cast<int64_t *>(labels)[i] = bj;
             else
                 reinterpret_cast<int32_t *>(labels)[i] = bj;
-            if (update) {
+            if (update && use_fx) {
+                // the packed terms into the integer totals; a flagged term
+                // (not representable) as its exact float value
+                const int64_t ds = d4 + 4;
+                const float wv = w[i];
+                for (int64_t j = 0; j <= d4; ++j) {
+                    const int pk = fx.xq[i * ds + j];
+                    const int64_t e = j < d4 ? (int64_t)bj * d4 + j : k * d4 + bj;
+                    if (pk == 1) {
+                        const float v = j < d4 ? __fmul_rn(xrow[i * d4 + j], wv) : wv;
+                        atomicAdd(j < d4 ? acc64 + (int64_t)bj * d4 + j : acc64 + k_pad * d4 + bj,
+                                  (double)v);
+                    } else if (pk != 0) {
+                        fx_add(fx, e, (long long)(pk >> 6) << ((pk >> 1) & 31));
+                    }
+                }
+            } else if (update) {
                 const float4 *xr = reinterpret_cast<const float4 *>(xrow + i * d4);
                 const float wv = w[i];
                 if (acc_f64) {
@@ -1585,8 +1635,8 @@ __global__ void __launch_bounds__(256) combine_kernel(
 // sums and sizes in dataT: copies added in index order in fp64, rounded once.
 template <typename A>
 __global__ void km_to_dk_kernel(const A *copies, int n_copies, float *out_c, float *out_sizes,
-                                int64_t d, int64_t k, int64_t k_pad, int64_t d4,
-                                const LoopState *guard) {
+                                int64_t d, int64_t k, int64_t k_pad, int64_t d4, FxAcc fx,
+                                const MixedConsts *consts, const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
     const int64_t cs = k_pad * d4 + k_pad;
     // consecutive threads read consecutive words of every copy
@@ -1596,8 +1646,18 @@ __global__ void km_to_dk_kernel(const A *copies, int n_copies, float *out_c, flo
         const int64_t off = is_size ? k_pad * d4 + (e - k * d4) : e;
         const int64_t j = e / d4, f = e % d4;
         if (!is_size && f >= d) continue;
-        // copies added in index order; loads issued eight ahead of the adds
+        // the integer totals (exact to one rounding), then the copies added
+        // in index order; loads issued eight ahead of the adds
         double acc = 0.0;
+        if (fx.hi != nullptr && consts->fx_ok) {
+            long long h = 0;
+            unsigned long long l = 0;
+            for (int c = 0; c < fx.copies; ++c) {
+                h += fx.hi[(int64_t)c * fx.stride + e];
+                l += fx.lo[(int64_t)c * fx.stride + e];
+            }
+            acc = ((double)h * 4294967296.0 + (double)l) * (1.0 / (double)pow2f(consts->fx_shift));
+        }
         int c = 0;
         for (; c + 8 <= n_copies; c += 8) {
             A v[8];
@@ -1615,7 +1675,7 @@ __global__ void km_to_dk_kernel(const A *copies, int n_copies, float *out_c, flo
 }
 
 __global__ void reset_kernel(float *sums32, double *acc64, int64_t count, int acc_f64,
-                             int *n_flagged, const LoopState *guard) {
+                             int *n_flagged, FxAcc fx, int64_t fx_count, const LoopState *guard) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -1624,6 +1684,12 @@ __global__ void reset_kernel(float *sums32, double *acc64, int64_t count, int ac
         else
             sums32[e] = 0.f;
     }
+    if (fx.hi != nullptr)
+        for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+             e < fx_count * fx.copies; e += (int64_t)gridDim.x * blockDim.x) {
+            fx.hi[e] = 0;
+            fx.lo[e] = 0ull;
+        }
     if (blockIdx.x == 0 && threadIdx.x == 0) *n_flagged = 0;
 }
 
@@ -1739,6 +1805,12 @@ struct MixedFit : PlainFit<float, I> {
     int64_t own_k = 0;  // > 0: fixed-point sums accumulated per CTA in shared memory
     int own_f = 1;      // packed columns per update thread in those sums
     int *xq = nullptr;  // [n][d4 + 4] packed fixed-point terms
+    long long *fxhi = nullptr;           // their integer totals (high words)
+    unsigned long long *fxlo = nullptr;  // (low words)
+    FxAcc fx_acc() const {
+        return own_k > 0 ? FxAcc{xq, fxhi, fxlo, this->prm.k * d4 + this->prm.k, n_copies}
+                         : FxAcc{nullptr, nullptr, nullptr, 0, 1};
+    }
 
     static bool supported(int64_t d, int64_t k) {
         const int nk = (int)ceil_div<int64_t>(std::max<int64_t>(d, 1), 64);
@@ -1810,6 +1882,9 @@ struct MixedFit : PlainFit<float, I> {
         const size_t o_a64 = take(acc_f64 ? sizeof(double) * csz : 16);
         const size_t o_xf = take(sizeof(float) * std::max<int64_t>(p.n, 1) * d4);
         const size_t o_xq = take(own_k > 0 ? sizeof(int) * std::max<int64_t>(p.n, 1) * (d4 + 4) : 16);
+        const size_t o_fx = take(own_k > 0 ? 2 * sizeof(long long) * (size_t)n_copies *
+                                                 (size_t)(p.k * d4 + p.k)
+                                           : 16);
         const size_t o_cn2 = take(sizeof(float) * p.k);
         const size_t o_dcn = take(sizeof(float) * p.k);
         const size_t o_cst = take(sizeof(MixedConsts));
@@ -1830,6 +1905,10 @@ struct MixedFit : PlainFit<float, I> {
         acc64 = reinterpret_cast<double *>(b + o_a64);
         xrow = reinterpret_cast<float *>(b + o_xf);
         xq = reinterpret_cast<int *>(b + o_xq);
+        if (own_k > 0) {
+            fxhi = reinterpret_cast<long long *>(b + o_fx);
+            fxlo = reinterpret_cast<unsigned long long *>(fxhi + n_copies * (p.k * d4 + p.k));
+        }
         cn2 = reinterpret_cast<float *>(b + o_cn2);
         dcn = reinterpret_cast<float *>(b + o_dcn);
         consts = reinterpret_cast<MixedConsts *>(b + o_cst);
@@ -1900,7 +1979,8 @@ struct MixedFit : PlainFit<float, I> {
         KMC_TRY(centroid_prep(cur, guard));
         const int64_t csz = (int64_t)n_copies * (k_pad * d4 + k_pad);
         reset_kernel<<<grid1d(csz, 256, 4096), 256, 0, s>>>(sums32, acc64, csz, acc_f64,
-                                                           n_flagged, guard);
+                                                           n_flagged, fx_acc(), p.k * d4 + p.k,
+                                                           guard);
         KMC_TRY(check_launch("mixed_reset"));
         MixedArgs a;
         a.ximg = ximg;
@@ -1941,6 +2021,7 @@ struct MixedFit : PlainFit<float, I> {
         a.own_k = a.multi ? 0 : own_k;
         a.own_f = own_f;
         a.xq = xq;
+        a.fx = fx_acc();
         const SmemLayout L = smem_layout(nkb, pass_cols, d4, stages, a.own_k, a.own_f);
         if ((L.ostage & 15) != 0 || (L.osum & 15) != 0) {
             set_error("mixed form: misaligned shared-memory sums layout");
@@ -1977,7 +2058,8 @@ struct MixedFit : PlainFit<float, I> {
             1, std::min<int64_t>((int64_t)num_sms() * 8, ceil_div<int64_t>(p.n, kRecheckThreads)));
         recheck_kernel<<<(unsigned)rgrid, kRecheckThreads, 0, s>>>(
             xrow, ct, this->hn, p.w, cand, flagged, n_flagged, p.n, p.d, p.k, d4, p.labels,
-            a.label64, update, acc_f64, sums32, acc64, k_pad, n_copies, guard, passes, pass_cols);
+            a.label64, update, acc_f64, sums32, acc64, k_pad, n_copies, guard, passes, pass_cols,
+            fx_acc(), consts);
         KMC_TRY(check_launch("mixed_recheck"));
         stats_kernel<<<1, 1, 0, s>>>(n_flagged, stats, stats + 1, guard);
         return check_launch("mixed_stats");
@@ -1993,10 +2075,12 @@ struct MixedFit : PlainFit<float, I> {
         cudaStream_t s = p.stream;
         if (acc_f64)
             km_to_dk_kernel<double><<<grid1d(p.k * d4 + p.k, 256, 4096), 256, 0, s>>>(
-                acc64, n_copies, nxt, this->sizes, p.d, p.k, k_pad, d4, this->state);
+                acc64, n_copies, nxt, this->sizes, p.d, p.k, k_pad, d4, fx_acc(), consts,
+                this->state);
         else
             km_to_dk_kernel<float><<<grid1d(p.k * d4 + p.k, 256, 4096), 256, 0, s>>>(
-                sums32, n_copies, nxt, this->sizes, p.d, p.k, k_pad, d4, this->state);
+                sums32, n_copies, nxt, this->sizes, p.d, p.k, k_pad, d4,
+                FxAcc{nullptr, nullptr, nullptr, 0, 1}, consts, this->state);
         KMC_TRY(check_launch("km_to_dk"));
         return launch_empty_list<float, I>(this->sizes, this->empty_list, this->n_empty, p.k, s,
                                            this->state);

@@ -234,6 +234,44 @@ def test_mixed_fixed_point_sums_with_tiny_values_and_weights(oracle, d, k, form)
         capi.check(L.kmc_fit_destroy(fit))
 
 
+# Up to 32 features the cluster sums are integer totals, added in any order to
+# the same bits: two runs of a fit give bit-identical centroids and labels.
+@pytest.mark.parametrize("d,k", [(8, 30), (32, 64)])
+def test_mixed_fixed_point_fits_are_bit_reproducible(d, k):
+    import torch
+
+    from kmeans_dpcpp_gb300 import capi
+
+    n = 400_000
+    X, _, _ = bench.make_blobs(n, d, k, (-5, 5), 1.0, 17)
+    C0 = np.ascontiguousarray(bench.random_row_init(X, k, 17))
+    rng = np.random.default_rng(17)
+    w = rng.uniform(0.25, 4.0, n).astype(np.float32)
+    L = capi.lib()
+    Xg = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+    wg = torch.from_numpy(w).cuda()
+    stream = torch.cuda.current_stream()
+    outs = []
+    for _ in range(2):
+        cur = torch.from_numpy(C0.copy()).cuda()
+        res = torch.empty_like(cur)
+        lab = torch.empty(n, dtype=torch.int32, device="cuda")
+        fit = ctypes.c_void_p()
+        capi.check(L.kmc_fit_create_f32_i32(Xg.data_ptr(), wg.data_ptr(), cur.data_ptr(), lab.data_ptr(),
+                                            res.data_ptr(), n, d, k, 0.0, 12, FORMS["fp16"],
+                                            stream.cuda_stream, ctypes.byref(fit)))
+        try:
+            capi.check(L.kmc_fit_run(fit))
+            it, inr = ctypes.c_int64(), ctypes.c_double()
+            capi.check(L.kmc_fit_finalize(fit, ctypes.byref(it), ctypes.byref(inr)))
+        finally:
+            capi.check(L.kmc_fit_destroy(fit))
+        outs.append((it.value, res.cpu().numpy(), lab.cpu().numpy()))
+    assert outs[0][0] == outs[1][0]
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+    np.testing.assert_array_equal(outs[0][2], outs[1][2])
+
+
 def test_fit_after_trimming_the_memory_pool_gives_the_same_labels(oracle):
     """Scratch comes from a pool that keeps freed memory mapped; trimming it
     between fits hands the memory back and the next fit allocates afresh."""

@@ -252,8 +252,9 @@ def test_budget_and_invalid_calls():
 def test_many_concurrent_mixed_sessions_all_finish_and_match_single_fits():
     """Dozens of tensor-core sessions of small, uneven fits run at once (their
     kernels on several streams).  Every fit must finish without a device-side
-    wait running out, and up to 32 features (exact sums) give the same labels
-    and centroids as the same fit run alone."""
+    wait running out, and up to 32 features (integer cluster sums, the same bits
+    in any order) give bit-identical labels and centroids to the same fit run
+    alone."""
     import torch
 
     from kmeans_dpcpp_gb300 import capi
@@ -295,5 +296,6 @@ def test_many_concurrent_mixed_sessions_all_finish_and_match_single_fits():
         finally:
             capi.check(L.kmc_fit_destroy(fit))
         out = r.result()
+        # integer (fixed-point) cluster sums: the same bits in any order
         np.testing.assert_array_equal(out["labels"], lab.cpu().numpy())
-        np.testing.assert_allclose(out["C"], res.cpu().numpy(), rtol=1e-6, atol=1e-6)
+        np.testing.assert_array_equal(out["C"], res.cpu().numpy())
