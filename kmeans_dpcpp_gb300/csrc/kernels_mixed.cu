@@ -50,12 +50,17 @@
 //   warp 1      TMEM allocation; one thread issues tcgen05.mma (M=128, N=256,
 //               K=16) into two 256-column TMEM accumulators
 //   warps 2-9   epilogue: tcgen05.ld of score pairs, P1/P2, certification, labels
-//   warps 10-11 update: w*x of certified samples into cluster-major sums in
-//               global memory, with fire-and-forget reductions
-//               (red.global.add.v4.f32, or red.global.add.f64 per feature
-//               when d <= 32) into the private copy of this CTA (copy
-//               blockIdx % n_copies), summed in copy order afterwards
+//   warps 10-11 update: w*x of certified samples into cluster-major sums.
+//               d > 32: fire-and-forget red.global.add.v4.f32 into the
+//               private copy of this CTA (copy blockIdx % n_copies), summed in
+//               copy order afterwards.  d <= 32: integer (fixed-point) sums
+//               in shared memory from terms packed once per fit, added at the
+//               end into order-independent integer totals (fixed_sums_role);
+//               when those sums do not fit shared memory,
+//               red.global.add.f64 per feature into the CTA's copy
 // Samples that fail certification are accumulated by the recheck kernel.
+// Waits poll mbarrier.test_wait (no suspension: with tensor-core kernels of
+// several streams at once, suspended waiters sometimes slept for seconds).
 //
 // Every wait is bounded.  A wait that runs out raises the CTA's error flag;
 // the other roles see it and stop, the producer and the MMA issuer then wait
