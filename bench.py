@@ -88,7 +88,7 @@ FORMS = {"plain": 0, "mixed-bf16": 1, "mixed-fp16": 2}
 # workload's shape (profiles/mixed_assign_c3_n1M.txt and
 # profiles/tile_kernel_plain_c3_n1M.txt); the kernels stream every sample
 # once, so a launch's traffic scales with n.
-TRAFFIC_PER_SAMPLE = {("c3", "mixed-fp16"): 404.5, ("c3", "plain"): 267.6}
+TRAFFIC_PER_SAMPLE = {("c3", "mixed-fp16"): 404.9, ("c3", "plain"): 267.6}
 
 
 # ---------------------------------------------------------------------------
