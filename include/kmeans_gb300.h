@@ -512,6 +512,20 @@ int kmc_fit_set_wait_limit(kmc_fit_t fit, int64_t clocks, int stall_once);
 int kmc_fit_tile_variant(int64_t n_features, int64_t n_clusters, int dtype_bytes,
                          kmc_stream_t stream, int *variant_out);
 int kmc_fit_set_tile_variant(kmc_fit_t fit, int variant);
+/* Mixed forms: the session's kernel variant, 10 * ring stages + f, where f = 4
+ * or 2 is the fixed-point cluster sums with that many columns per update
+ * thread and f = 0 the float reductions (-1 for a plain session).  The
+ * autotuner times the variants that fit shared memory on a synthetic fit once
+ * per (n_features, power-of-two bucket of n_clusters, form, size class: at
+ * least 32 128-sample tiles per SM or fewer), caches the fastest beside the
+ * tile choices above (KMC_TUNE=0: the deepest ring with the widest
+ * fixed-point sums).  Every variant gives the same labels.
+ * kmc_debug_force_mixed_variant forces a variant for the fits created
+ * afterwards (a test hook; -1 restores the tuner; a variant that does not fit
+ * a shape fails that fit with KMC_ERR_INVALID_ARGUMENT).  No reference
+ * counterpart. */
+int kmc_fit_mixed_variant(kmc_fit_t fit, int *variant_out);
+int kmc_debug_force_mixed_variant(int variant);
 /* Kernel launches enqueued so far by this session. */
 int kmc_fit_launch_count(kmc_fit_t fit, int64_t *launches_out);
 int kmc_fit_destroy(kmc_fit_t fit);

@@ -501,6 +501,12 @@ int kmc_fit_tile_variant(int64_t n_features, int64_t n_clusters, int dtype_bytes
                                                               variant_out);
     return kmc::tune_fit_variant<double>(n_features, n_clusters, S(stream), variant_out);
 }
+int kmc_fit_mixed_variant(kmc_fit_t fit, int *variant_out) {
+    KMC_FIT_CHECK(fit);
+    KMC_CHECK_ARG(variant_out != nullptr, "null output pointer");
+    return kmc::mixed_variant_of(fit->impl, variant_out);
+}
+int kmc_debug_force_mixed_variant(int variant) { return kmc::force_mixed_variant(variant); }
 int kmc_fit_launch_count(kmc_fit_t fit, int64_t *out) {
     KMC_FIT_CHECK(fit);
     KMC_CHECK_ARG(out != nullptr, "null output pointer");

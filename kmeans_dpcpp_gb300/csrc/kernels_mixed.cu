@@ -72,8 +72,11 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
+#include <vector>
 
+#include "km_batch.cuh"
 #include "km_fit.cuh"
 #include "km_mixed.cuh"
 
@@ -1766,6 +1769,111 @@ unsigned grid1d(int64_t work, int block, int cap = 8192) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// Mixed-form variant choice.  A variant forced process-wide (a test hook) or
+// for the fits the autotuner creates on this thread overrides the tuner.
+std::atomic<int> g_force_mixed_variant{-1};
+thread_local int tl_force_mixed_variant = -1;
+
+int forced_variant() {
+    const int g = g_force_mixed_variant.load();
+    return g >= 0 ? g : tl_force_mixed_variant;
+}
+
+int64_t pow2_at_least(int64_t v) {
+    int64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+template <typename I>
+int make_mixed_fit_impl(const FitParams<float, I> &p, int form, std::unique_ptr<FitBase> *out);
+
+// Times each candidate variant on a synthetic fit (Gaussian blobs of d
+// features, k clusters) for four iterations after one warm-up, and caches the
+// fastest per (d, k, form, size class).  Fits of at least 32 tiles per SM
+// ("large") are timed with 48 tiles per SM, smaller ones with 8: the
+// per-CTA costs of the fixed-point sums (zeroing and adding the shared-memory
+// copies) weigh on few tiles, not on many.  KMC_TUNE=0 keeps the default (the
+// first candidate).
+int tune_mixed_variant(int64_t d, int64_t k, int form, bool large, const std::vector<int> &cand,
+                       cudaStream_t s, int *code) {
+    *code = cand.front();
+    if (const char *e = std::getenv("KMC_TUNE"))
+        if (e[0] == '0') return KMC_OK;
+    const char *tag = form == KMC_FORM_MIXED_BF16 ? (large ? "mixed-bf16-large" : "mixed-bf16")
+                                                  : (large ? "mixed-fp16-large" : "mixed-fp16");
+    int cached = -1;
+    if (tune_lookup(d, k, tag, &cached) &&
+        std::find(cand.begin(), cand.end(), cached) != cand.end()) {
+        *code = cached;
+        return KMC_OK;
+    }
+    const int64_t n = (int64_t)num_sms() * kTileM * (large ? 48 : 8);
+    Scratch mem;
+    const size_t oX = 0, oC0 = oX + align256(sizeof(float) * n * d);
+    const size_t oC = oC0 + align256(sizeof(float) * d * k), oCn = oC + align256(sizeof(float) * d * k);
+    const size_t ow = oCn + align256(sizeof(float) * d * k), ol = ow + align256(sizeof(float) * n);
+    const size_t oi = ol + align256(sizeof(int32_t) * n);
+    KMC_TRY(mem.alloc(oi + align256(sizeof(int32_t) * k), s));
+    char *b = mem.as<char>();
+    float *X = reinterpret_cast<float *>(b + oX), *C0 = reinterpret_cast<float *>(b + oC0);
+    float *C = reinterpret_cast<float *>(b + oC), *Cn = reinterpret_cast<float *>(b + oCn);
+    float *w = reinterpret_cast<float *>(b + ow);
+    int32_t *lab = reinterpret_cast<int32_t *>(b + ol), *idx = reinterpret_cast<int32_t *>(b + oi);
+    KMC_TRY(launch_blobs(X, n, d, k, -10.f, 10.f, 1.f, 1.f, 77, s));
+    KMC_TRY(launch_fill<float>(w, 1.f, n, s));
+    std::vector<int32_t> rows;
+    seeded_rows(n, k, 78, &rows);
+    KMC_CUDA_TRY(cudaMemcpyAsync(idx, rows.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, s));
+    KMC_TRY(launch_gather_rows(X, n, d, idx, k, C0, s));
+    KMC_CUDA_TRY(cudaStreamSynchronize(s));  // rows (host vector) copied
+    cudaEvent_t e0, e1;
+    KMC_CUDA_TRY(cudaEventCreate(&e0));
+    KMC_CUDA_TRY(cudaEventCreate(&e1));
+    float best_ms = 0.f;
+    int best = -1;
+    for (int c : cand) {
+        FitParams<float, int32_t> q;
+        q.X = X;
+        q.w = w;
+        q.centroids = C;
+        q.new_centroids = Cn;
+        q.labels = lab;
+        q.n = n;
+        q.d = d;
+        q.k = k;
+        q.tol = 0.0;
+        q.max_iter = 1000;
+        q.stream = s;
+        if (cudaMemcpyAsync(C, C0, sizeof(float) * d * k, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            continue;
+        tl_force_mixed_variant = c;
+        std::unique_ptr<FitBase> fit;
+        int rc = make_mixed_fit_impl<int32_t>(q, form, &fit);
+        tl_force_mixed_variant = -1;
+        if (rc != KMC_OK) continue;
+        float ms = 0.f;
+        rc = fit->enqueue_iteration();
+        if (rc == KMC_OK) rc = cudaEventRecord(e0, s) == cudaSuccess ? KMC_OK : KMC_ERR_CUDA;
+        for (int it = 0; it < 4 && rc == KMC_OK; ++it) rc = fit->enqueue_iteration();
+        if (rc == KMC_OK) rc = cudaEventRecord(e1, s) == cudaSuccess ? KMC_OK : KMC_ERR_CUDA;
+        if (rc == KMC_OK) rc = cudaEventSynchronize(e1) == cudaSuccess ? KMC_OK : KMC_ERR_CUDA;
+        if (rc == KMC_OK) rc = cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess ? KMC_OK : KMC_ERR_CUDA;
+        if (rc == KMC_OK && (best < 0 || ms < best_ms)) {
+            best_ms = ms;
+            best = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    KMC_CUDA_TRY(cudaStreamSynchronize(s));
+    if (best >= 0) {
+        tune_record(d, k, tag, best);
+        *code = best;
+    }
+    return KMC_OK;
+}
+
 template <typename I>
 struct MixedFit : PlainFit<float, I> {
     using Base = PlainFit<float, I>;
@@ -1807,6 +1915,7 @@ struct MixedFit : PlainFit<float, I> {
     int nch = 1;     // 256-column chunks per pass
     int passes = 1;  // column passes per assignment (n_clusters beyond one pass)
     float *pmax = nullptr;
+    int variant = 0;    // 10 stages + fixed-point columns per thread (0: none)
     int64_t own_k = 0;  // > 0: fixed-point sums accumulated per CTA in shared memory
     int own_f = 1;      // packed columns per update thread in those sums
     int *xq = nullptr;  // [n][d4 + 4] packed fixed-point terms
@@ -1851,15 +1960,43 @@ struct MixedFit : PlainFit<float, I> {
         // read-modify-write chain (one row after another) is slower than the
         // float64 reductions.  Fits only: a prediction has no weights and no
         // sums.
-        if (acc_f64 && passes == 1 && p.w != nullptr) {
-            for (int st = stages; st >= 2 && own_k == 0; --st)
-                for (int f : {4, 2})
-                    if (smem_layout(nkb, k_pad, d4, st, p.k, f).total <= kSmemLimit) {
-                        own_k = p.k;
-                        own_f = f;
-                        stages = st;
-                        break;
-                    }
+        //
+        // The choice (ring depth, and for these sums fixed point with 4 or 2
+        // columns per thread or float64 reductions) is a variant code
+        // 10 stages + f (f = 0: no fixed point).  The autotuner times the
+        // variants that fit on a synthetic fit once per (d, power-of-two
+        // bucket of k, form, size class) and caches the fastest; the rule
+        // above is the default when tuning is off.
+        {
+            std::vector<int> cand;
+            const int64_t kb = std::min<int64_t>(k_pad, std::max<int64_t>(pow2_at_least(p.k), 1));
+            const bool fx_shape = acc_f64 && passes == 1 && p.w != nullptr;
+            for (int st = stages; st >= 2; --st) {
+                if (fx_shape)
+                    for (int f : {4, 2})
+                        if (smem_layout(nkb, k_pad, d4, st, kb, f).total <= kSmemLimit)
+                            cand.push_back(10 * st + f);
+                if (smem_layout(nkb, k_pad, d4, st).total <= kSmemLimit) cand.push_back(10 * st);
+            }
+            if (cand.empty()) cand.push_back(10 * stages);
+            int code = cand.front();  // deepest ring, widest fixed-point sums
+            const int forced = forced_variant();
+            if (forced >= 0) {
+                if (std::find(cand.begin(), cand.end(), forced) == cand.end()) {
+                    set_error("mixed form: variant %d does not fit this shape", forced);
+                    return KMC_ERR_INVALID_ARGUMENT;
+                }
+                code = forced;
+            } else if (cand.size() > 1) {
+                const bool large = ntiles >= 32 * (int64_t)num_sms();
+                KMC_TRY(tune_mixed_variant(p.d, kb, form, large, cand, s, &code));
+            }
+            variant = code;
+            stages = code / 10;
+            if (code % 10 != 0) {
+                own_k = p.k;
+                own_f = code % 10;
+            }
         }
         size_t off = 0;
         auto take = [&](size_t bytes) {
@@ -2108,23 +2245,41 @@ struct MixedFit : PlainFit<float, I> {
     }
 };
 
+template <typename I>
+int make_mixed_fit_impl(const FitParams<float, I> &p, int form, std::unique_ptr<FitBase> *out) {
+    if (!MixedFit<I>::supported(p.d, p.k)) {
+        set_error("mixed form supports n_features <= %d (got d=%lld, k=%lld)",
+                  64 * kMaxFeatureBlocks, (long long)p.d, (long long)p.k);
+        return KMC_ERR_UNSUPPORTED;
+    }
+    auto f = std::make_unique<MixedFit<I>>();
+    KMC_TRY(f->init(p));
+    KMC_TRY(f->init_mixed(form));
+    *out = std::move(f);
+    return KMC_OK;
+}
+
 template <typename T, typename I>
 int make_mixed_fit(const FitParams<T, I> &p, int form, std::unique_ptr<FitBase> *out) {
     if constexpr (!std::is_same<T, float>::value) {
         set_error("the mixed tensor-core form needs float32 data");
         return KMC_ERR_UNSUPPORTED;
     } else {
-        if (!MixedFit<I>::supported(p.d, p.k)) {
-            set_error("mixed form supports n_features <= %d (got d=%lld, k=%lld)",
-                      64 * kMaxFeatureBlocks, (long long)p.d, (long long)p.k);
-            return KMC_ERR_UNSUPPORTED;
-        }
-        auto f = std::make_unique<MixedFit<I>>();
-        KMC_TRY(f->init(p));
-        KMC_TRY(f->init_mixed(form));
-        *out = std::move(f);
-        return KMC_OK;
+        return make_mixed_fit_impl<I>(p, form, out);
     }
+}
+
+int force_mixed_variant(int code) {
+    KMC_CHECK_ARG(code == -1 || (code >= 10 && code <= 44), "variant must be -1 or 10 s + f");
+    g_force_mixed_variant.store(code);
+    return KMC_OK;
+}
+
+int mixed_variant_of(FitBase *fit, int *code) {
+    auto *m32 = dynamic_cast<MixedFit<int32_t> *>(fit);
+    auto *m64 = dynamic_cast<MixedFit<int64_t> *>(fit);
+    *code = m32 ? m32->variant : (m64 ? m64->variant : -1);
+    return KMC_OK;
 }
 
 bool mixed_fit_supported(int64_t d, int64_t k) { return MixedFit<int32_t>::supported(d, k); }

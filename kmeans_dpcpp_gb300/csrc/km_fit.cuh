@@ -146,5 +146,10 @@ template <typename T, typename I>
 int make_mixed_fit(const FitParams<T, I> &p, int form, std::unique_ptr<FitBase> *out);
 // Whether the mixed form takes n_features = d and n_clusters = k.
 bool mixed_fit_supported(int64_t d, int64_t k);
+// Mixed-form variant (10 stages + fixed-point columns per update thread, 0 for
+// float reductions): forced for every fit created afterwards (-1: the
+// autotuner's choice again), and a session's choice (-1: not a mixed fit).
+int force_mixed_variant(int code);
+int mixed_variant_of(FitBase *fit, int *code);
 
 }  // namespace kmc

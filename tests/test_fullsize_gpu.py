@@ -129,3 +129,34 @@ def test_c2_whole_trajectory_equals_oracle(kdp, oracle, dt):
         assert _near_tie(X, C_o, i), f"sample {i} differs without a near-tie"
     np.testing.assert_allclose(C_g, C_o, rtol=RTOL[dt], atol=RTOL[dt] * np.abs(C_o).max())
     assert float(inertia[0]) == pytest.approx(inr_o, rel=RTOL[dt])
+
+
+# The c2 configuration in the mixed form (d = 14: the tensor-core assignment
+# with the fixed-point integer cluster sums): the whole 100-iteration
+# trajectory equals the oracle's as in the plain form.
+@pytest.mark.parametrize("form", ["mixed-fp16", "mixed-bf16"])
+def test_c2_mixed_whole_trajectory_equals_oracle(kdp, oracle, form):
+    import torch
+
+    n, d, k = 5_000_000, 14, 127
+    X, _, _ = bench.make_blobs(n, d, k, (-10, 10), 1.5, 1)
+    C0 = bench.random_row_init(X, k, 1, far_first=True)
+    it_o, lab_o, C_o, inr_o, rel_o = oracle.kmeans_lloyd_driver(X, np.ones(n, np.float32), C0, 0.0, 100)
+    assert rel_o >= 1
+
+    Xg = torch.from_numpy(X).cuda()
+    w = torch.ones(n, dtype=Xg.dtype, device="cuda")
+    init = torch.from_numpy(C0.copy()).cuda()
+    res_c = torch.empty_like(init)
+    lab = torch.empty(n, dtype=torch.int32, device="cuda")
+    it_g, inertia = kdp.kmeans_lloyd_driver(Xg, w, init, lab, res_c, 0.0, False, 100, 8, 128, 0.7, None,
+                                            form=form)
+    lab_g, C_g = lab.cpu().numpy(), res_c.cpu().numpy()
+
+    assert it_g == it_o
+    bad = np.flatnonzero(lab_g != lab_o)
+    assert bad.size <= 16, f"{bad.size} labels differ"
+    for i in bad:
+        assert _near_tie(X, C_o, i), f"sample {i} differs without a near-tie"
+    np.testing.assert_allclose(C_g, C_o, rtol=RTOL[np.float32], atol=RTOL[np.float32] * np.abs(C_o).max())
+    assert float(inertia[0]) == pytest.approx(inr_o, rel=RTOL[np.float32])

@@ -93,3 +93,98 @@ def test_tuner_choice_is_cached(tmp_path):
             del os.environ["KMC_TILE_CACHE"]
         else:
             os.environ["KMC_TILE_CACHE"] = old
+
+
+# ---------------------------------------------------------------------------
+# Mixed forms: the kernel variant (ring depth, and up to 32 features the
+# fixed-point cluster sums with 4 or 2 columns per update thread or float
+# reductions) is chosen by the same autotuner.  Every variant must give a fit
+# whose final labels are the exact float32 labels of its centroids and whose
+# centroids follow the oracle; the fixed-point variants (integer sums) give
+# bit-identical centroids.
+MIXED_FP16 = 2
+
+
+def _mixed_fit(L, capi, X, C0, max_iter):
+    import torch
+
+    d, n = X.shape
+    k = C0.shape[1]
+    Xg = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+    w = torch.ones(n, dtype=torch.float32, device="cuda")
+    cur = torch.from_numpy(C0.copy()).cuda()
+    res = torch.empty_like(cur)
+    lab = torch.empty(n, dtype=torch.int32, device="cuda")
+    fit = ctypes.c_void_p()
+    rc = L.kmc_fit_create_f32_i32(Xg.data_ptr(), w.data_ptr(), cur.data_ptr(), lab.data_ptr(),
+                                  res.data_ptr(), n, d, k, 0.0, max_iter, MIXED_FP16,
+                                  torch.cuda.current_stream().cuda_stream, ctypes.byref(fit))
+    if rc != 0:
+        return rc, None
+    try:
+        v = ctypes.c_int()
+        capi.check(L.kmc_fit_mixed_variant(fit, ctypes.byref(v)))
+        capi.check(L.kmc_fit_run(fit))
+        it, inr = ctypes.c_int64(), ctypes.c_double()
+        capi.check(L.kmc_fit_finalize(fit, ctypes.byref(it), ctypes.byref(inr)))
+    finally:
+        capi.check(L.kmc_fit_destroy(fit))
+    return 0, (v.value, it.value, lab.cpu().numpy(), res.cpu().numpy())
+
+
+@pytest.mark.parametrize("n,d,k", [(60_000, 16, 40), (50_000, 32, 100), (40_000, 64, 200)])
+def test_mixed_variants_give_the_same_fit(oracle, n, d, k):
+    from kmeans_dpcpp_gb300 import capi
+
+    L = capi.lib()
+    X, _, _ = bench.make_blobs(n, d, k, (-10, 10), 1.0, n + d)
+    C0 = np.ascontiguousarray(bench.random_row_init(X, k, n + d))
+    iters = 2
+    _, _, C_o, _, _ = oracle.kmeans_lloyd_driver(X, np.ones(n, np.float32), C0, 0.0, iters)
+    runs = {}
+    try:
+        for code in [10 * s + f for s in (4, 3, 2) for f in (4, 2, 0)]:
+            capi.check(L.kmc_debug_force_mixed_variant(code))
+            rc, out = _mixed_fit(L, capi, X, C0, iters)
+            if rc == 1:  # this variant does not fit the shape
+                continue
+            capi.check(rc)
+            runs[code] = out
+    finally:
+        capi.check(L.kmc_debug_force_mixed_variant(-1))
+    assert len(runs) >= 2 if d <= 32 else len(runs) >= 1
+    fixed = []
+    for code, (v, it, lab, C) in runs.items():
+        assert v == code and it == iters
+        np.testing.assert_array_equal(lab, oracle.assignment(X, C))
+        np.testing.assert_allclose(C, C_o, rtol=1e-5, atol=1e-5 * np.abs(C_o).max())
+        if code % 10:
+            fixed.append(C)
+    for C in fixed[1:]:
+        np.testing.assert_array_equal(C, fixed[0])
+    if d <= 32:
+        assert fixed, "no fixed-point variant fits"
+
+
+def test_mixed_tuner_choice_is_cached(tmp_path):
+    from kmeans_dpcpp_gb300 import capi
+
+    L = capi.lib()
+    cache = tmp_path / "tiles.txt"
+    old = os.environ.get("KMC_TILE_CACHE")
+    os.environ["KMC_TILE_CACHE"] = str(cache)
+    try:
+        X, _, _ = bench.make_blobs(30_000, 24, 16, (-10, 10), 1.0, 5)
+        out = []
+        for k in (77, 100):  # the same bucket (128)
+            C0 = np.ascontiguousarray(bench.random_row_init(X, k, 5))
+            rc, res = _mixed_fit(L, capi, X, C0, 1)
+            capi.check(rc)
+            out.append(res[0])
+        assert out[0] == out[1] and out[0] // 10 in (2, 3, 4) and out[0] % 10 in (0, 2, 4)
+        assert cache.read_text().split("\n").count(f"24 128 mixed-fp16 {out[0]}") == 1
+    finally:
+        if old is None:
+            del os.environ["KMC_TILE_CACHE"]
+        else:
+            os.environ["KMC_TILE_CACHE"] = old
