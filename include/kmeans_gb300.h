@@ -519,7 +519,8 @@ int kmc_fit_set_tile_variant(kmc_fit_t fit, int variant);
  * per (n_features, power-of-two bucket of n_clusters, form, size class: at
  * least 32 128-sample tiles per SM or fewer), caches the fastest beside the
  * tile choices above (KMC_TUNE=0: the deepest ring with the widest
- * fixed-point sums).  Every variant gives the same labels.
+ * fixed-point sums).  Sessions of the request server use a cached choice or
+ * that default and never time variants on a request's path.  Every variant gives the same labels.
  * kmc_debug_force_mixed_variant forces a variant for the fits created
  * afterwards (a test hook; -1 restores the tuner; a variant that does not fit
  * a shape fails that fit with KMC_ERR_INVALID_ARGUMENT).  No reference

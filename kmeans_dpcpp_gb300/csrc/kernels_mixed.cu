@@ -1773,6 +1773,9 @@ unsigned grid1d(int64_t work, int block, int cap = 8192) {
 // for the fits the autotuner creates on this thread overrides the tuner.
 std::atomic<int> g_force_mixed_variant{-1};
 thread_local int tl_force_mixed_variant = -1;
+// Fits created while this is set use a cached choice or the default, never
+// time variants (the request server: no measurement on a request's path).
+thread_local bool tl_mixed_lookup_only = false;
 
 int forced_variant() {
     const int g = g_force_mixed_variant.load();
@@ -1808,6 +1811,7 @@ int tune_mixed_variant(int64_t d, int64_t k, int form, bool large, const std::ve
         *code = cached;
         return KMC_OK;
     }
+    if (tl_mixed_lookup_only) return KMC_OK;
     const int64_t n = (int64_t)num_sms() * kTileM * (large ? 48 : 8);
     Scratch mem;
     const size_t oX = 0, oC0 = oX + align256(sizeof(float) * n * d);
@@ -2268,6 +2272,8 @@ int make_mixed_fit(const FitParams<T, I> &p, int form, std::unique_ptr<FitBase> 
         return make_mixed_fit_impl<I>(p, form, out);
     }
 }
+
+void mixed_tuning_lookup_only(bool on) { tl_mixed_lookup_only = on; }
 
 int force_mixed_variant(int code) {
     KMC_CHECK_ARG(code == -1 || (code >= 10 && code <= 44), "variant must be -1 or 10 s + f");

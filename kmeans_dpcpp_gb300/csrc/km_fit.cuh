@@ -150,6 +150,9 @@ bool mixed_fit_supported(int64_t d, int64_t k);
 // float reductions): forced for every fit created afterwards (-1: the
 // autotuner's choice again), and a session's choice (-1: not a mixed fit).
 int force_mixed_variant(int code);
+// Fits created on this thread while on use cached variant choices or the
+// default and never time variants (the request server).
+void mixed_tuning_lookup_only(bool on);
 int mixed_variant_of(FitBase *fit, int *code);
 
 }  // namespace kmc

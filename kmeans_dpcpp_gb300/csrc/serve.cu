@@ -747,7 +747,11 @@ struct Server {
             p.tol = t.kind == 0 ? t.tol : 0.0;
             p.max_iter = t.kind == 0 ? t.max_iter : 0;
             p.stream = a->st;
-            KMC_TRY(make_mixed_fit<float, int32_t>(p, form, &a->fit));
+            // a cached variant choice or the default: no timing on a request's path
+            mixed_tuning_lookup_only(true);
+            const int mrc = make_mixed_fit<float, int32_t>(p, form, &a->fit);
+            mixed_tuning_lookup_only(false);
+            KMC_TRY(mrc);
             a->slot = free_slots.back();
             free_slots.pop_back();
             a->hstate = reinterpret_cast<LoopState *>(pinned + kSlotBytes * (size_t)a->slot);
