@@ -174,15 +174,16 @@ def test_mixed_tuner_choice_is_cached(tmp_path):
     old = os.environ.get("KMC_TILE_CACHE")
     os.environ["KMC_TILE_CACHE"] = str(cache)
     try:
-        X, _, _ = bench.make_blobs(30_000, 24, 16, (-10, 10), 1.0, 5)
+        # a shape no other test uses, so the choice is not already in memory
+        X, _, _ = bench.make_blobs(30_000, 19, 16, (-10, 10), 1.0, 5)
         out = []
-        for k in (77, 100):  # the same bucket (128)
+        for k in (37, 50):  # the same bucket (64)
             C0 = np.ascontiguousarray(bench.random_row_init(X, k, 5))
             rc, res = _mixed_fit(L, capi, X, C0, 1)
             capi.check(rc)
             out.append(res[0])
         assert out[0] == out[1] and out[0] // 10 in (2, 3, 4) and out[0] % 10 in (0, 2, 4)
-        assert cache.read_text().split("\n").count(f"24 128 mixed-fp16 {out[0]}") == 1
+        assert cache.read_text().split("\n").count(f"19 64 mixed-fp16 {out[0]}") == 1
     finally:
         if old is None:
             del os.environ["KMC_TILE_CACHE"]
