@@ -1512,7 +1512,7 @@ __global__ void __launch_bounds__(kRecheckThreads) recheck_kernel(
                         atomicAdd(j < d4 ? acc64 + (int64_t)bj * d4 + j : acc64 + k_pad * d4 + bj,
                                   (double)v);
                     } else if (pk != 0) {
-                        fx_add(fx, e, (long long)(pk >> 6) << ((pk >> 1) & 31));
+                        fx_add(fx, e, (long long)(pk >> 6) * (1ll << ((pk >> 1) & 31)));
                     }
                 }
             } else if (update) {
