@@ -220,6 +220,7 @@ int fused_step(const T *X, const T *w, const T *C, const T *hn, I *lab, T *sums,
 
 template <typename T, typename I>
 int make_fit(const FitParams<T, I> &p, int form, std::unique_ptr<FitBase> *out) {
+    Range range("kmc.fit_create");
     if (form == KMC_FORM_PLAIN) {
         auto f = std::make_unique<PlainFit<T, I>>();
         KMC_TRY(f->init(p));
@@ -235,6 +236,7 @@ template <typename T, typename I>
 int driver(const T *X, const T *w, T *init_c, I *labels, T *res_c, int64_t n, int64_t d,
            int64_t k, double tol, int verbose, int64_t max_iter, double occ, cudaStream_t s,
            kmc_print_fn pf, void *pctx, int64_t *n_iter_out, T *inertia_out) {
+    Range range("kmc.lloyd_driver");
     CHECK_DIMS(n, d, k, max_iter);
     KMC_CHECK_ARG(occ > 0.0 && occ < 1.0,
                   "Fraction `centroids_private_copies_max_cache_occupancy` is out of bounds");
@@ -447,12 +449,14 @@ KMC_FIT_CREATE_ROWMAJOR(f64_i64, double, int64_t)
 #define KMC_FIT_CHECK(fit) KMC_CHECK_ARG((fit) != nullptr && (fit)->impl != nullptr, "null fit")
 
 int kmc_fit_step(kmc_fit_t fit, int64_t n_iterations) {
+    kmc::Range range("kmc.fit_step");
     KMC_FIT_CHECK(fit);
     KMC_CHECK_ARG(n_iterations >= 0, "n_iterations must be non-negative");
     for (int64_t t = 0; t < n_iterations; ++t) KMC_TRY(fit->impl->enqueue_iteration());
     return KMC_OK;
 }
 int kmc_fit_run(kmc_fit_t fit) {
+    kmc::Range range("kmc.fit_run");
     KMC_FIT_CHECK(fit);
     return fit->impl->run(0);
 }
@@ -466,6 +470,7 @@ int kmc_fit_status(kmc_fit_t fit, int64_t *n_iter, int *done, double *last_shift
     return KMC_OK;
 }
 int kmc_fit_finalize(kmc_fit_t fit, int64_t *n_iter, double *inertia) {
+    kmc::Range range("kmc.fit_finalize");
     KMC_FIT_CHECK(fit);
     return fit->impl->finalize(n_iter, inertia);
 }

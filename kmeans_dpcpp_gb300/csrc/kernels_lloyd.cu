@@ -452,6 +452,7 @@ __global__ void tune_fill_kernel(T *x, int64_t count, uint64_t seed) {
 
 template <typename T>
 int tune_fit_variant(int64_t d, int64_t k_in, cudaStream_t s, int *variant) {
+    Range range("kmc.tune_fit_variant");
     *variant = 0;
     if (const char *e = std::getenv("KMC_TUNE"))
         if (e[0] == '0') return KMC_OK;

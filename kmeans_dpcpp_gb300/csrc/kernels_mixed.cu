@@ -1800,6 +1800,7 @@ int make_mixed_fit_impl(const FitParams<float, I> &p, int form, std::unique_ptr<
 // first candidate).
 int tune_mixed_variant(int64_t d, int64_t k, int form, bool large, const std::vector<int> &cand,
                        cudaStream_t s, int *code) {
+    Range range("kmc.tune_mixed_variant");
     *code = cand.front();
     if (const char *e = std::getenv("KMC_TUNE"))
         if (e[0] == '0') return KMC_OK;

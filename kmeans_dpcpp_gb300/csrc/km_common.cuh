@@ -11,10 +11,35 @@
 #include <limits>
 #include <string>
 #include <cuda_runtime.h>
+#if __has_include(<nvtx3/nvToolsExt.h>)
+#include <nvtx3/nvToolsExt.h>
+#define KMC_HAVE_NVTX 1
+#endif
 
 #include "../../include/kmeans_gb300.h"
 
 namespace kmc {
+
+// A named NVTX range for the duration of a scope: profilers (ncu, Nsight
+// Systems) show the library's phases -- fit creation (operand conversion,
+// autotuning), the Lloyd loop, the final pass, serving steps.  NVTX is
+// header-only and costs nothing unless a tool is attached.
+struct Range {
+    explicit Range(const char *name) {
+#ifdef KMC_HAVE_NVTX
+        nvtxRangePushA(name);
+#else
+        (void)name;
+#endif
+    }
+    ~Range() {
+#ifdef KMC_HAVE_NVTX
+        nvtxRangePop();
+#endif
+    }
+    Range(const Range &) = delete;
+    Range &operator=(const Range &) = delete;
+};
 
 // ---------------------------------------------------------------------------
 // Error reporting.  The C-ABI never throws; every entry point returns a status

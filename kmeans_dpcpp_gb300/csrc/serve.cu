@@ -930,6 +930,7 @@ struct Server {
     }
 
     int progress(bool *moved) {
+        Range range("kmc.server_progress");
         *moved = false;
         KMC_TRY(admit(moved));
         if (plain)
@@ -1150,6 +1151,7 @@ int kmc_batch_step(kmc_batch_t batch, int64_t *n_active_out) {
 }
 
 int kmc_batch_run(kmc_batch_t batch) {
+    kmc::Range range("kmc.batch_run");
     KMC_CHECK_ARG(batch != nullptr, "null batch");
     int64_t active = 1;
     while (active > 0) KMC_TRY(batch->eng.step(&active));
