@@ -263,6 +263,28 @@ def dist_setup(n_gpus):
     return world, rank, local
 
 
+def gpu_local_cpus(local):
+    """Host CPUs next to GPU `local` (its PCI device's local_cpulist), or None."""
+    import torch
+
+    try:
+        p = torch.cuda.get_device_properties(local)
+        bus = "%04x:%02x:%02x.0" % (p.pci_domain_id, p.pci_bus_id, p.pci_device_id)
+        with open("/sys/bus/pci/devices/%s/local_cpulist" % bus) as f:
+            text = f.read().strip()
+        cpus = set()
+        for part in text.split(","):
+            if "-" in part:
+                a, b = part.split("-")
+                cpus.update(range(int(a), int(b) + 1))
+            elif part:
+                cpus.add(int(part))
+        cpus &= os.sched_getaffinity(0)
+        return cpus or None
+    except Exception:
+        return None
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -731,11 +753,22 @@ def run_gb300(args, world, rank, local):
     # ---- end to end through the drop-in surface, host buffers ----
     e2e = None
     if not args.no_e2e:
-        X_h = torch.from_numpy(X_t).pin_memory()
-        w_h = torch.ones(n, dtype=Xg.dtype).pin_memory()
-        C_h = torch.from_numpy(C0.copy()).pin_memory()
-        lab_h = torch.empty(n, dtype=torch.int32).pin_memory()
-        Cres_h = torch.empty_like(C_h).pin_memory()
+        # The pinned host buffers are allocated and filled from the CPUs next
+        # to the GPU, so their pages sit on the GPU's side of the host (a
+        # caller placing its buffers would do the same); the affinity is
+        # restored afterwards.
+        saved = os.sched_getaffinity(0)
+        near = gpu_local_cpus(local)
+        if near:
+            os.sched_setaffinity(0, near)
+        try:
+            X_h = torch.from_numpy(X_t).pin_memory()
+            w_h = torch.ones(n, dtype=Xg.dtype).pin_memory()
+            C_h = torch.from_numpy(C0.copy()).pin_memory()
+            lab_h = torch.empty(n, dtype=torch.int32).pin_memory()
+            Cres_h = torch.empty_like(C_h).pin_memory()
+        finally:
+            os.sched_setaffinity(0, saved)
         Xd = torch.empty_like(Xg)
         wd = torch.empty_like(wg)
         Cd = torch.from_numpy(C0.copy()).cuda()
@@ -748,17 +781,24 @@ def run_gb300(args, world, rank, local):
         wd.copy_(w_h, non_blocking=True)
         Cd.copy_(C_h, non_blocking=True)
         torch.cuda.current_stream().synchronize()
+        t1 = time.perf_counter()
         n_iter, inertia = kdp.kmeans_lloyd_driver(Xd, wd, Cd, labd, Crd, 0.0, False, args.steps, 8, 128,
                                                   0.7, None, form=form)
+        t2 = time.perf_counter()
         lab_h.copy_(labd)
         Cres_h.copy_(Crd)
         torch.cuda.synchronize()
-        t_e2e = all_max(world, time.perf_counter() - t0)
+        t3 = time.perf_counter()
+        t_e2e = all_max(world, t3 - t0)
         assert n_iter == args.steps
         h2d = X_t.nbytes + X_t.itemsize * n + C0.nbytes
         d2h = 4 * n + C0.nbytes + X_t.itemsize
         e2e = {"value": world * n_iter / t_e2e, "unit": "iter/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h,
+               "host_buffers_on_cpus": (("%d CPUs local to the GPU" % len(near)) if near
+                                        else "not placed (no local CPU list)"),
+               "split_ms": {"h2d": 1e3 * (t1 - t0), "driver_call": 1e3 * (t2 - t1),
+                            "d2h": 1e3 * (t3 - t2)},
                "note": "one kmeans_lloyd_driver call (form=%s) of K iterations (tol=0): pinned-host "
                        "copies of X, weights, init centroids in and labels, centroids, inertia out, "
                        "plus the one-time operand conversion; bytes are per call" % form}
