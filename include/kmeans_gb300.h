@@ -527,6 +527,14 @@ int kmc_fit_set_tile_variant(kmc_fit_t fit, int variant);
  * counterpart. */
 int kmc_fit_mixed_variant(kmc_fit_t fit, int *variant_out);
 int kmc_debug_force_mixed_variant(int variant);
+/* The packed fixed-point term the mixed forms use for the cluster sums up to
+ * 32 features (host copy of the packing, for tests; no GPU involved): for
+ * value = +-m 2^(E - 150) (E its exponent field, m its 24-bit mantissa) and
+ * scale 2^shift, packed = (+-m) << 6 | (E - 150 + shift) << 1 when that shift
+ * is 0..30 (then value 2^shift = +-m 2^(E - 150 + shift) exactly), 0 for a
+ * zero, and the flag 1 otherwise (too small for the scale, denormal, infinite,
+ * NaN).  No reference counterpart. */
+int kmc_debug_pack_fixed(float value, int shift, int *packed_out);
 /* Kernel launches enqueued so far by this session. */
 int kmc_fit_launch_count(kmc_fit_t fit, int64_t *launches_out);
 int kmc_fit_destroy(kmc_fit_t fit);

@@ -512,6 +512,12 @@ int kmc_fit_mixed_variant(kmc_fit_t fit, int *variant_out) {
     return kmc::mixed_variant_of(fit->impl, variant_out);
 }
 int kmc_debug_force_mixed_variant(int variant) { return kmc::force_mixed_variant(variant); }
+int kmc_debug_pack_fixed(float value, int shift, int *packed_out) {
+    KMC_CHECK_ARG(packed_out != nullptr, "null output pointer");
+    KMC_CHECK_ARG(shift >= -74 && shift <= 100, "shift out of range");
+    *packed_out = kmc::pack_fixed_term(value, shift);
+    return KMC_OK;
+}
 int kmc_fit_launch_count(kmc_fit_t fit, int64_t *out) {
     KMC_FIT_CHECK(fit);
     KMC_CHECK_ARG(out != nullptr, "null output pointer");

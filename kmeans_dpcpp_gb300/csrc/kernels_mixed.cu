@@ -2291,6 +2291,8 @@ int mixed_variant_of(FitBase *fit, int *code) {
 
 bool mixed_fit_supported(int64_t d, int64_t k) { return MixedFit<int32_t>::supported(d, k); }
 
+int pack_fixed_term(float v, int shift) { return pack_fixed(v, 150 - shift); }
+
 template int make_mixed_fit<float, int32_t>(const FitParams<float, int32_t> &, int,
                                             std::unique_ptr<FitBase> *);
 template int make_mixed_fit<float, int64_t>(const FitParams<float, int64_t> &, int,

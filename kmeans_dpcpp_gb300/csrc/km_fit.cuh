@@ -153,6 +153,9 @@ int force_mixed_variant(int code);
 // Fits created on this thread while on use cached variant choices or the
 // default and never time variants (the request server).
 void mixed_tuning_lookup_only(bool on);
+// The packed fixed-point term of v at scale 2^shift (host copy of the
+// device's packing, for tests).
+int pack_fixed_term(float v, int shift);
 int mixed_variant_of(FitBase *fit, int *code);
 
 }  // namespace kmc
