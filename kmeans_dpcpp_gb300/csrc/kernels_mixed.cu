@@ -140,6 +140,27 @@ __device__ __forceinline__ void fx_add(const FxAcc &fx, int64_t e, long long q) 
     atomicAdd(fx.lo + e, (unsigned long long)(q & 0xffffffffll));
 }
 
+// Sample i (label c) into the integer totals of fx (this block's copy): its
+// packed terms w x_j (j < d4) and w; a flagged term (not representable) goes
+// as its exact float value into the float64 copy acc64 ([k_pad][d4] sums,
+// then k_pad sizes).
+__device__ __forceinline__ void add_packed_row(const FxAcc &fx, double *acc64, int64_t k_pad,
+                                               int64_t k, int64_t d4, const float *xrow,
+                                               const float *w, int64_t i, int64_t c) {
+    const int64_t ds = d4 + 4;
+    const float wv = w[i];
+    for (int64_t j = 0; j <= d4; ++j) {
+        const int pk = fx.xq[i * ds + j];
+        if (pk == 1) {
+            const float v = j < d4 ? __fmul_rn(xrow[i * d4 + j], wv) : wv;
+            atomicAdd(j < d4 ? acc64 + c * d4 + j : acc64 + k_pad * d4 + c, (double)v);
+        } else if (pk != 0) {
+            fx_add(fx, j < d4 ? c * d4 + j : k * d4 + c,
+                   (long long)(pk >> 6) * (1ll << ((pk >> 1) & 31)));
+        }
+    }
+}
+
 struct MixedArgs {
     const uint8_t *ximg;
     const uint8_t *cimg;
@@ -1500,21 +1521,7 @@ __global__ void __launch_bounds__(kRecheckThreads) recheck_kernel(
             else
                 reinterpret_cast<int32_t *>(labels)[i] = bj;
             if (update && use_fx) {
-                // the packed terms into the integer totals; a flagged term
-                // (not representable) as its exact float value
-                const int64_t ds = d4 + 4;
-                const float wv = w[i];
-                for (int64_t j = 0; j <= d4; ++j) {
-                    const int pk = fx.xq[i * ds + j];
-                    const int64_t e = j < d4 ? (int64_t)bj * d4 + j : k * d4 + bj;
-                    if (pk == 1) {
-                        const float v = j < d4 ? __fmul_rn(xrow[i * d4 + j], wv) : wv;
-                        atomicAdd(j < d4 ? acc64 + (int64_t)bj * d4 + j : acc64 + k_pad * d4 + bj,
-                                  (double)v);
-                    } else if (pk != 0) {
-                        fx_add(fx, e, (long long)(pk >> 6) * (1ll << ((pk >> 1) & 31)));
-                    }
-                }
+                add_packed_row(fx, acc64, k_pad, k, d4, xrow, w, i, bj);
             } else if (update) {
                 const float4 *xr = reinterpret_cast<const float4 *>(xrow + i * d4);
                 const float wv = w[i];
@@ -1558,9 +1565,11 @@ __global__ void __launch_bounds__(256) combine_kernel(
     const float *ndx, const MixedConsts *consts, const float *xrow, const float *w, void *labels,
     int label64, int update, int acc_f64, float *sums32, double *acc64, int64_t k_pad,
     int64_t d4, int n_copies, int *flagged, int *n_flagged, int64_t n, int64_t k,
-    const LoopState *guard) {
+    const LoopState *guard, FxAcc fx) {
     if (guard != nullptr && *reinterpret_cast<const volatile int *>(&guard->done)) return;
     const MixedConsts cst = *consts;
+    const bool use_fx = fx.xq != nullptr && cst.fx_ok;
+    fx = fx.copy_of(blockIdx.x);
     {
         const int64_t copy = (int64_t)(blockIdx.x % (unsigned)n_copies) * (k_pad * d4 + k_pad);
         sums32 += copy;
@@ -1605,7 +1614,9 @@ __global__ void __launch_bounds__(256) combine_kernel(
                 reinterpret_cast<int64_t *>(labels)[i] = label;
             else
                 reinterpret_cast<int32_t *>(labels)[i] = (int32_t)label;
-            if (update) {
+            if (update && use_fx) {
+                add_packed_row(fx, acc64, k_pad, k, d4, xrow, w, i, label);
+            } else if (update) {
                 const float4 *xr = reinterpret_cast<const float4 *>(xrow + i * d4);
                 const float wv = w[i];
                 if (acc_f64) {
@@ -1926,9 +1937,13 @@ struct MixedFit : PlainFit<float, I> {
     int *xq = nullptr;  // [n][d4 + 4] packed fixed-point terms
     long long *fxhi = nullptr;           // their integer totals (high words)
     unsigned long long *fxlo = nullptr;  // (low words)
+    // Up to 32 features (fits with weights): packed terms and integer totals
+    // for every accumulating kernel -- the assignment's fixed-point sums when
+    // its variant has them, the recheck and the column passes' combine.
+    bool fx_on = false;
     FxAcc fx_acc() const {
-        return own_k > 0 ? FxAcc{xq, fxhi, fxlo, this->prm.k * d4 + this->prm.k, n_copies}
-                         : FxAcc{nullptr, nullptr, nullptr, 0, 1};
+        return fx_on ? FxAcc{xq, fxhi, fxlo, this->prm.k * d4 + this->prm.k, n_copies}
+                     : FxAcc{nullptr, nullptr, nullptr, 0, 1};
     }
 
     static bool supported(int64_t d, int64_t k) {
@@ -2028,8 +2043,9 @@ struct MixedFit : PlainFit<float, I> {
         const size_t o_s32 = take(acc_f64 ? 16 : sizeof(float) * csz);
         const size_t o_a64 = take(acc_f64 ? sizeof(double) * csz : 16);
         const size_t o_xf = take(sizeof(float) * std::max<int64_t>(p.n, 1) * d4);
-        const size_t o_xq = take(own_k > 0 ? sizeof(int) * std::max<int64_t>(p.n, 1) * (d4 + 4) : 16);
-        const size_t o_fx = take(own_k > 0 ? 2 * sizeof(long long) * (size_t)n_copies *
+        fx_on = acc_f64 && p.w != nullptr;
+        const size_t o_xq = take(fx_on ? sizeof(int) * std::max<int64_t>(p.n, 1) * (d4 + 4) : 16);
+        const size_t o_fx = take(fx_on ? 2 * sizeof(long long) * (size_t)n_copies *
                                                  (size_t)(p.k * d4 + p.k)
                                            : 16);
         const size_t o_cn2 = take(sizeof(float) * p.k);
@@ -2052,7 +2068,7 @@ struct MixedFit : PlainFit<float, I> {
         acc64 = reinterpret_cast<double *>(b + o_a64);
         xrow = reinterpret_cast<float *>(b + o_xf);
         xq = reinterpret_cast<int *>(b + o_xq);
-        if (own_k > 0) {
+        if (fx_on) {
             fxhi = reinterpret_cast<long long *>(b + o_fx);
             fxlo = reinterpret_cast<unsigned long long *>(fxhi + n_copies * (p.k * d4 + p.k));
         }
@@ -2074,7 +2090,7 @@ struct MixedFit : PlainFit<float, I> {
         KMC_TRY(check_launch("absmax"));
         sigma_kernel<<<1, 1, 0, s>>>(consts, bf16, p.d);
         KMC_TRY(check_launch("sigma"));
-        if (own_k > 0) {
+        if (fx_on) {
             absmax_kernel<<<grid1d(p.n, 256, 4096), 256, 0, s>>>(p.w, p.n, &consts->wmax_bits);
             KMC_TRY(check_launch("absmax_w"));
             // rows one CTA of the assignment handles at most
@@ -2096,7 +2112,7 @@ struct MixedFit : PlainFit<float, I> {
         }
         KMC_TRY(check_launch("x_image"));
         this->launches += 3;
-        if (own_k > 0) {
+        if (fx_on) {
             fx_pack_kernel<<<grid1d(p.n * (d4 + 4), 256, 8192), 256, 0, s>>>(xrow, p.w, p.n, d4,
                                                                            consts, xq);
             KMC_TRY(check_launch("fx_pack"));
@@ -2195,7 +2211,7 @@ struct MixedFit : PlainFit<float, I> {
                 combine_kernel<<<grid1d(p.n, 256, num_sms() * 8), 256, 0, s>>>(
                     pmax, cand, passes, pass_cols, nx, ndx, consts, xrow, p.w, p.labels, a.label64,
                     update, acc_f64, sums32, acc64, k_pad, d4, n_copies, flagged, n_flagged, p.n,
-                    p.k, guard);
+                    p.k, guard, fx_acc());
                 KMC_TRY(check_launch("mixed_combine"));
             }
         }

@@ -235,8 +235,9 @@ def test_mixed_fixed_point_sums_with_tiny_values_and_weights(oracle, d, k, form)
 
 
 # Up to 32 features the cluster sums are integer totals, added in any order to
-# the same bits: two runs of a fit give bit-identical centroids and labels.
-@pytest.mark.parametrize("d,k", [(8, 30), (32, 64)])
+# the same bits: two runs of a fit give bit-identical centroids and labels
+# (k = 1500 takes two column passes, whose combine adds the integer totals).
+@pytest.mark.parametrize("d,k", [(8, 30), (32, 64), (16, 1500)])
 def test_mixed_fixed_point_fits_are_bit_reproducible(d, k):
     import torch
 
