@@ -2008,8 +2008,11 @@ struct MixedFit : PlainFit<float, I> {
                 }
                 code = forced;
             } else if (cand.size() > 1) {
+                // a measurement that cannot run (out of memory, say) leaves the
+                // default: tuning never fails a fit
                 const bool large = ntiles >= 32 * (int64_t)num_sms();
-                KMC_TRY(tune_mixed_variant(p.d, kb, form, large, cand, s, &code));
+                if (tune_mixed_variant(p.d, kb, form, large, cand, s, &code) != KMC_OK)
+                    code = cand.front();
             }
             variant = code;
             stages = code / 10;
