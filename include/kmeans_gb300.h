@@ -619,6 +619,15 @@ int kmc_generate_blobs_f32(float *X_t, int64_t n_samples, int64_t n_features,
                            float std_hi, uint64_t seed, kmc_stream_t stream);
 /* Seeded distinct row indices for random-row initialisation (host). */
 int kmc_seeded_rows(int64_t n_samples, int64_t n_clusters, uint64_t seed, int32_t *rows_out);
+/* The batched engine's work items for instances of n_samples[q] samples, mode
+ * modes[q] (0 fit, 1 assign, 2 transform) and tile variant variants[q] (host
+ * planning only, for tests): runs of at most 8 128-sample tiles, listed by
+ * group (kind * 3 + variant; kind 1 = transforms) in instance order.  Writes up
+ * to `capacity` items and the total count.  No reference counterpart. */
+int kmc_debug_batch_items(int64_t count, const int64_t *n_samples, const int *modes,
+                          const int *variants, int64_t capacity, int32_t *instance_out,
+                          int32_t *tiles_out, int64_t *first_tile_out, int32_t *group_out,
+                          int64_t *n_items_out);
 
 /* ---- serving loop ------------------------------------------------------------------
  * No counterpart in the reference.  Replays a stream of fit and predict

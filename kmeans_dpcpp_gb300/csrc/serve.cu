@@ -33,6 +33,20 @@ namespace {
 
 constexpr int kItemTiles = 8;  // 128-sample tiles per work item
 
+// Work items of one instance: runs of at most kItemTiles 128-sample tiles,
+// appended to the list of its (kind, tile variant); kind 1 = distance
+// (transform) instances, 0 = the rest.  The persistent assign kernels take
+// items from a device counter (atomicAdd), so every tile is handled by one
+// CTA exactly once.
+void append_items(int q, int64_t n, int mode, int variant,
+                  std::vector<BItem> (&items)[2][kBatchVariants]) {
+    const int64_t tiles = ceil_div<int64_t>(n, kBatchTileM);
+    const int kind = (mode == B_TRANSFORM) ? 1 : 0;
+    for (int64_t t = 0; t < tiles; t += kItemTiles)
+        items[kind][variant].push_back(
+            BItem{q, (int)std::min<int64_t>(kItemTiles, tiles - t), (long long)t});
+}
+
 // Engine-owned device memory of one instance.
 struct SlotMem {
     Scratch mem;
@@ -280,11 +294,7 @@ struct BatchEngine {
             const BInst &h = tab[(size_t)q];
             all.push_back((int)q);
             if (h.mode == B_FIT) fits.push_back((int)q);
-            const int64_t tiles = ceil_div<int64_t>(h.n, kBatchTileM);
-            const int kind = (h.mode == B_TRANSFORM) ? 1 : 0;
-            for (int64_t t = 0; t < tiles; t += kItemTiles)
-                items[kind][h.variant].push_back(
-                    BItem{(int)q, (int)std::min<int64_t>(kItemTiles, tiles - t), (long long)t});
+            append_items((int)q, h.n, h.mode, h.variant, items);
         }
         int64_t total = 0;
         for (int kind = 0; kind < 2; ++kind)
@@ -1206,6 +1216,36 @@ int kmc_generate_blobs_f32(float *X_t, int64_t n_samples, int64_t n_features,
     KMC_CHECK_ARG(n_samples >= 0 && n_features >= 0, "negative dimension");
     return launch_blobs(X_t, n_samples, n_features, n_centers, box_lo, box_hi, std_lo, std_hi,
                         seed, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int kmc_debug_batch_items(int64_t count, const int64_t *n_samples, const int *modes,
+                          const int *variants, int64_t capacity, int32_t *instance_out,
+                          int32_t *tiles_out, int64_t *first_tile_out, int32_t *group_out,
+                          int64_t *n_items_out) {
+    KMC_CHECK_ARG(count >= 0 && n_items_out != nullptr, "invalid arguments");
+    KMC_CHECK_ARG(count == 0 || (n_samples && modes && variants), "null input");
+    std::vector<kmc::BItem> items[2][kmc::kBatchVariants];
+    for (int64_t q = 0; q < count; ++q) {
+        KMC_CHECK_ARG(n_samples[q] >= 0 && variants[q] >= 0 && variants[q] < kmc::kBatchVariants &&
+                          modes[q] >= kmc::B_FIT && modes[q] <= kmc::B_TRANSFORM,
+                      "invalid instance %lld", (long long)q);
+        kmc::append_items((int)q, n_samples[q], modes[q], variants[q], items);
+    }
+    int64_t total = 0;
+    for (int kind = 0; kind < 2; ++kind)
+        for (int v = 0; v < kmc::kBatchVariants; ++v) {
+            for (const kmc::BItem &it : items[kind][v]) {
+                if (total < capacity) {
+                    instance_out[total] = it.inst;
+                    tiles_out[total] = it.ntiles;
+                    first_tile_out[total] = it.tile0;
+                    group_out[total] = kind * kmc::kBatchVariants + v;
+                }
+                ++total;
+            }
+        }
+    *n_items_out = total;
+    return KMC_OK;
 }
 
 int kmc_seeded_rows(int64_t n_samples, int64_t n_clusters, uint64_t seed, int32_t *rows_out) {

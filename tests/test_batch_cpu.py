@@ -58,3 +58,64 @@ def test_serve_run_rejects_bad_request_streams(rows, msg):
     rc = L.kmc_serve_run(_reqs(rows), len(rows), 0, 1 << 30, 8, None, res, ctypes.byref(mk))
     assert rc == 1
     assert msg in L.kmc_last_error().decode()
+
+
+def test_work_items_cover_every_tile_once_under_concurrent_pulls():
+    """A mocked work queue on CPU threads: the engine's own planner
+    (kmc_debug_batch_items) splits uneven instances into items; eight threads
+    take items from a shared counter, as the persistent assign CTAs do with
+    their device counter, and every 128-sample tile of every instance must be
+    handled exactly once, in the group of its kind and tile variant."""
+    import itertools
+    import threading
+
+    L = capi.lib()
+    rng = np.random.default_rng(3)
+    count = 40
+    n = rng.integers(0, 300_000, count).astype(np.int64)
+    n[:3] = [0, 1, 128 * 8 + 1]           # empty, one sample, just past one item
+    modes = rng.integers(0, 3, count).astype(np.int32)
+    variants = rng.integers(0, 3, count).astype(np.int32)
+    total = ctypes.c_int64()
+    P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))  # noqa: E731
+    capi.check(L.kmc_debug_batch_items(count, P(n, ctypes.c_int64), P(modes, ctypes.c_int),
+                                       P(variants, ctypes.c_int), 0, None, None, None, None,
+                                       ctypes.byref(total)))
+    m = total.value
+    inst = np.empty(m, np.int32)
+    tiles = np.empty(m, np.int32)
+    first = np.empty(m, np.int64)
+    group = np.empty(m, np.int32)
+    capi.check(L.kmc_debug_batch_items(count, P(n, ctypes.c_int64), P(modes, ctypes.c_int),
+                                       P(variants, ctypes.c_int), m, P(inst, ctypes.c_int32),
+                                       P(tiles, ctypes.c_int32), P(first, ctypes.c_int64),
+                                       P(group, ctypes.c_int32), ctypes.byref(total)))
+    assert np.all((tiles >= 1) & (tiles <= 8))
+    assert np.all(group == (modes[inst] == 2) * 3 + variants[inst])
+    assert np.all(np.diff(group) >= 0)     # listed group by group
+
+    seen = [np.zeros(-(-int(v) // 128), np.int32) for v in n]
+    lock = threading.Lock()
+    for g in np.unique(group):
+        idx = np.flatnonzero(group == g)
+        counter = itertools.count()
+
+        def worker():
+            while True:
+                with lock:
+                    j = next(counter)
+                if j >= len(idx):
+                    return
+                it = idx[j]
+                s = seen[inst[it]]
+                for t in range(first[it], first[it] + tiles[it]):
+                    with lock:
+                        s[t] += 1
+
+        threads = [threading.Thread(target=worker) for _ in range(8)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+    for q in range(count):
+        assert np.all(seen[q] == 1), q
