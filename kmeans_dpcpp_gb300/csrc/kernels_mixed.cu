@@ -412,27 +412,21 @@ __device__ __forceinline__ void add_packed(unsigned long long &sum, int p) {
     asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(sum) : "r"(ms), "r"(pw));
 }
 
-// own_f consecutive 64-bit sums at a shared-window address (16-byte aligned
-// for own_f >= 2).
+// own_f (2 or 4) consecutive 64-bit sums at a 16-byte aligned shared-window
+// address (volatile: kept in program order with each other).
 template <int F>
 __device__ __forceinline__ void lds_sums(uint32_t addr, unsigned long long (&q)[F]) {
-    if constexpr (F == 1) {
-        q[0] = lds_b64(addr);
-    } else {
+    static_assert(F == 2 || F == 4, "two or four columns per thread");
 #pragma unroll
-        for (int j = 0; j < F; j += 2)
-            asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(q[j]), "=l"(q[j + 1]) : "r"(addr + 8u * j));
-    }
+    for (int j = 0; j < F; j += 2)
+        asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(q[j]), "=l"(q[j + 1]) : "r"(addr + 8u * j));
 }
 template <int F>
 __device__ __forceinline__ void sts_sums(uint32_t addr, const unsigned long long (&q)[F]) {
-    if constexpr (F == 1) {
-        sts_b64(addr, q[0]);
-    } else {
+    static_assert(F == 2 || F == 4, "two or four columns per thread");
 #pragma unroll
-        for (int j = 0; j < F; j += 2)
-            asm volatile("st.shared.v2.u64 [%0], {%1, %2};" ::"r"(addr + 8u * j), "l"(q[j]), "l"(q[j + 1]));
-    }
+    for (int j = 0; j < F; j += 2)
+        asm volatile("st.shared.v2.u64 [%0], {%1, %2};" ::"r"(addr + 8u * j), "l"(q[j]), "l"(q[j + 1]));
 }
 
 // Second pass over a tile's terms that the fixed-point sums cannot hold
@@ -546,11 +540,9 @@ __device__ __forceinline__ void fixed_sums_role(const MixedArgs &a, const MixedC
                 if constexpr (F == 4) {
                     const int4 q = *reinterpret_cast<const int4 *>(t);
                     v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
-                } else if constexpr (F == 2) {
+                } else {
                     const int2 q = *reinterpret_cast<const int2 *>(t);
                     v[0] = q.x, v[1] = q.y;
-                } else {
-                    v[0] = t[0];
                 }
                 const uint32_t addr = mine + (uint32_t)c * cstride;
                 unsigned long long sum[F];

@@ -17,22 +17,6 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// Shared-memory loads and stores at 32-bit shared-window addresses (kept in
-// program order with each other).
-__device__ __forceinline__ uint32_t lds_b32(uint32_t addr) {
-    uint32_t v;
-    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(addr));
-    return v;
-}
-__device__ __forceinline__ unsigned long long lds_b64(uint32_t addr) {
-    unsigned long long v;
-    asm volatile("ld.shared.b64 %0, [%1];" : "=l"(v) : "r"(addr));
-    return v;
-}
-__device__ __forceinline__ void sts_b64(uint32_t addr, unsigned long long v) {
-    asm volatile("st.shared.b64 [%0], %1;" ::"r"(addr), "l"(v));
-}
-
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
                  : "memory");
