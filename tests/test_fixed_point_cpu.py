@@ -61,3 +61,37 @@ def test_pack_rejects_shifts_outside_the_window():
     out = ctypes.c_int()
     assert L.kmc_debug_pack_fixed(ctypes.c_float(1.0), 101, ctypes.byref(out)) == 1
     assert L.kmc_debug_pack_fixed(ctypes.c_float(1.0), -75, ctypes.byref(out)) == 1
+
+
+def test_high_low_totals_reassemble_the_exact_sum_in_any_order():
+    """The integer totals add each term q as (q >> 32) into a high word and
+    (q mod 2^32) into a low word (64-bit wrapping adds, as the device's
+    atomics); high 2^32 + low is the exact sum whatever the order, so the one
+    rounding to float64 gives the same bits for every order."""
+    capi, L = _lib()
+    rng = np.random.default_rng(7)
+    shift = 40
+    vals = (rng.standard_normal(20_000) * 7.0).astype(np.float32)
+    vals[:50] = 0.0
+    out = ctypes.c_int()
+    qs = []
+    for v in vals:
+        capi.check(L.kmc_debug_pack_fixed(ctypes.c_float(float(v)), shift, ctypes.byref(out)))
+        assert out.value != 1
+        qs.append(_unpack(out.value))
+    exact = sum(Fraction(float(v)) for v in vals) * Fraction(2) ** shift
+    assert exact == sum(qs)
+    M64 = (1 << 64) - 1
+    results = set()
+    for perm in range(4):
+        order = rng.permutation(len(qs))
+        hi = lo = 0
+        for i in order:
+            q = qs[i]
+            hi = (hi + (q >> 32)) & M64
+            lo = (lo + (q & 0xFFFFFFFF)) & M64
+        if hi >= 1 << 63:
+            hi -= 1 << 64          # the high word is a signed 64-bit integer
+        assert hi * 2 ** 32 + lo == sum(qs)
+        results.add((float(hi) * 4294967296.0 + float(lo)) * 2.0 ** -shift)
+    assert len(results) == 1
