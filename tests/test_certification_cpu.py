@@ -39,7 +39,7 @@ def _sigma(xmax, d, bf16):
     return s
 
 
-def _certified_labels(X, C, hn, bf16):
+def _certified_labels(X, C, hn, bf16, order="sequential"):
     d, n = X.shape
     k = C.shape[1]
     xmax = float(np.abs(X).max())
@@ -74,8 +74,18 @@ def _certified_labels(X, C, hn, bf16):
     # scores: exact 16-bit products accumulated in float32 over the features,
     # then the three norm terms -c_p h_p (exact products)
     acc = np.zeros((n, k), np.float32)
-    for f in range(d):
-        acc = (acc + np.outer(xs[f], cs[f]).astype(np.float32)).astype(np.float32)
+    if order == "sequential":
+        for f in range(d):
+            acc = (acc + np.outer(xs[f], cs[f]).astype(np.float32)).astype(np.float32)
+    else:
+        # K = 16 steps: each step's 16 products summed as a float32 tree, the
+        # step then added to the accumulator (another order the hardware may use)
+        for f0 in range(0, d, 16):
+            terms = [np.outer(xs[f], cs[f]).astype(np.float32) for f in range(f0, min(d, f0 + 16))]
+            while len(terms) > 1:
+                terms = [(terms[i] + terms[i + 1]).astype(np.float32) if i + 1 < len(terms)
+                         else terms[i] for i in range(0, len(terms), 2)]
+            acc = (acc + terms[0]).astype(np.float32)
     for c_p, part in zip(coef, (h0, h1, h2)):
         acc = (acc - (c_p * part).astype(np.float32)[None, :]).astype(np.float32)
     score = acc.astype(np.float64) / s2                       # x.c - hn, unscaled
@@ -99,10 +109,11 @@ def _near_ties(rng, n, d, k):
     return np.ascontiguousarray(X), np.ascontiguousarray(C)
 
 
+@pytest.mark.parametrize("order", ["sequential", "blocks16"])
 @pytest.mark.parametrize("bf16", [False, True])
 @pytest.mark.parametrize("kind", ["blobs", "near_ties"])
 @pytest.mark.parametrize("d,k", [(8, 16), (33, 40), (64, 64)])
-def test_certified_winners_are_the_exact_labels(oracle, bf16, kind, d, k):
+def test_certified_winners_are_the_exact_labels(oracle, bf16, kind, d, k, order):
     import bench
 
     rng = np.random.default_rng(d * 100 + k + (7 if bf16 else 0))
@@ -114,7 +125,7 @@ def test_certified_winners_are_the_exact_labels(oracle, bf16, kind, d, k):
         X, C = _near_ties(rng, n, d, k)
     hn = oracle.half_l2_norm_squared(C)
     ref = oracle.assignment(X, C)
-    cert, win = _certified_labels(X, C, hn, bf16)
+    cert, win = _certified_labels(X, C, hn, bf16, order)
     assert cert.mean() > (0.5 if kind == "blobs" else 0.2)
     bad = np.flatnonzero(cert & (win != ref))
     assert bad.size == 0, f"{bad.size} certified samples disagree with the exact labels"
